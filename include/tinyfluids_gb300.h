@@ -1,0 +1,143 @@
+/*
+ * tinyfluids_gb300 -- C ABI of the GB300 (sm_103a) tinyfluids time step.
+ *
+ * A drop-in for the reference's hot path, tinyfluids/jax_tinyfluids:
+ * the first-order Godunov / HLL update of the 3D compressible Euler
+ * equations (fluid.py) and its run-to-time loop (time_integration.py).
+ *
+ * Conventions shared by every entry point:
+ *  - A state is a device array of 5 * nx * ny * nz float32 in the
+ *    reference's layout [var][x][y][z], z contiguous, var order
+ *    rho, vx, vy, vz, p (fluid.py:10-22).  Conserved states use
+ *    rho, mx, my, mz, E.
+ *  - The caller owns all device memory; no entry point allocates device
+ *    memory.  Inputs are never modified; outputs must not alias inputs.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Work is
+ *    enqueued asynchronously unless stated otherwise.
+ *  - Every function returns a tf_status; tf_last_error() describes the last
+ *    failure on the calling thread.
+ *
+ * The reference has no FFI of its own (it is a JAX program); each entry
+ * point cites the reference function whose inputs, outputs and semantics it
+ * reproduces.
+ */
+#ifndef TINYFLUIDS_GB300_H
+#define TINYFLUIDS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TF_ABI_VERSION 1
+
+typedef enum tf_status {
+  TF_OK = 0,
+  TF_ERR_ARG = 1,          /* invalid argument (shape, pointer, value) */
+  TF_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+  TF_ERR_NONFINITE = 3,    /* the max wave speed became NaN/Inf/0: state blew up */
+  TF_ERR_TIMEOUT = 4,      /* a bounded device-side wait gave up */
+  TF_ERR_UNSUPPORTED = 5   /* valid request this build does not implement */
+} tf_status;
+
+/* flags */
+#define TF_FLAG_OPEN_BOUNDARIES 1u /* fluid.py:571-572 handle_boundaries=True */
+#define TF_FLAG_EXACT 2u           /* reference op order, bit-identical to the oracle */
+
+/*
+ * Device-resident control block of a run (64 bytes, caller-allocated device
+ * memory, tf_ctl_bytes()).  The run-to-time loop keeps t, dt and the
+ * iteration count here so that no host synchronisation is needed per step
+ * (the reference keeps them in the carry of lax.while_loop,
+ * time_integration.py:63-92).
+ */
+typedef struct tf_ctl {
+  float t;            /* simulated time reached */
+  float dt;           /* CFL dt of the current state (fluid.py:502) */
+  float t_final;      /* loop runs while t < t_final (time_integration.py:85-87) */
+  float cfl_dx;       /* C_CFL * dx rounded to float */
+  unsigned ws_bits;   /* internal: running max wave speed (float bits) */
+  unsigned done;      /* internal: finished-CTA counter */
+  int iter;           /* steps taken (the reference's num_iterations) */
+  int active;         /* nonzero while the loop condition holds */
+  int max_steps;      /* < 0: unbounded */
+  int status;         /* TF_OK or a device-detected tf_status */
+  float max_speed;    /* max wave speed of the current state */
+  int reserved[5];
+} tf_ctl;
+
+/* Tile shape of the fused step kernel; NULL = built-in heuristic. */
+typedef struct tf_tile_config {
+  int rows;  /* warps per CTA incl. the 2 halo rows: 8 or 16 */
+  int lx;    /* x planes per CTA (>= 1) */
+} tf_tile_config;
+
+int tf_abi_version(void);
+const char *tf_status_string(int status);
+const char *tf_last_error(void);
+unsigned long long tf_ctl_bytes(void);
+
+/* fluid.py:30-67 conserved_state_from_primitive.  W, U: 5*ncells floats. */
+int tf_conserved_from_primitive(const float *W, float *U, long long ncells, float gamma,
+                                void *stream);
+
+/* fluid.py:71-103 primitive_state_from_conserved. */
+int tf_primitive_from_conserved(const float *U, float *W, long long ncells, float gamma,
+                                void *stream);
+
+/* fluid.py:427-504 _cfl_time_step.  Writes ctl->dt = C_CFL*dx/max_speed and
+ * ctl->max_speed (device), resets the rest of ctl. */
+int tf_cfl_time_step(const float *W, int nx, int ny, int nz, float dx, float gamma,
+                     float cfl, tf_ctl *ctl, void *stream);
+
+/* fluid.py:562-578 _evolve_state: one split step with a given dt.  dt is
+ * read from dt_dev (device float) when non-NULL, else dt_host.  flags:
+ * TF_FLAG_OPEN_BOUNDARIES, TF_FLAG_EXACT.  tile may be NULL. */
+int tf_evolve_state(const float *W_in, float *W_out, int nx, int ny, int nz, float dx,
+                    float dt_host, const float *dt_dev, float gamma, unsigned flags,
+                    const tf_tile_config *tile, void *stream);
+
+/* time_integration.py:94-128 (plain branch): while t < t_final: dt = CFL dt;
+ * W = step(W, dt); t += dt; iter += 1.  max_steps >= 0 also bounds the loop
+ * (0 = t_final only is NOT implied: pass -1 for unbounded).  fixed_dt > 0
+ * replaces the CFL dt (the fixed-dt form used for differentiation).
+ * work: scratch state of the same size (ping-pong).  The final state is in
+ * W_out; ctl holds t, iter and status.  If iters_host is non-NULL the call
+ * blocks until the loop ends and stores the iteration count there; the
+ * t_final loop always synchronises once per chunk of steps to test the
+ * condition. */
+int tf_time_integration(const float *W_in, float *W_out, float *work, tf_ctl *ctl, int nx,
+                        int ny, int nz, float dx, float t_final, float gamma, float cfl,
+                        int max_steps, float fixed_dt, unsigned flags,
+                        const tf_tile_config *tile, int *iters_host, void *stream);
+
+/* Per-sweep form of fluid.py:508-557 (_evolve_state_along_axis), axis 0..2,
+ * on primitive states: reads W_in, writes W_out.  open_boundaries applies
+ * the fluid.py:571-572 remap to the input (use it for the x sweep only).
+ * Exact (reference op order) unless flags lacks TF_FLAG_EXACT, in which case
+ * the fast arithmetic is used.  A step equals the x, y, z sweeps in order. */
+int tf_evolve_along_axis(const float *W_in, float *W_out, int nx, int ny, int nz, float dx,
+                         float dt_host, const float *dt_dev, float gamma, int axis,
+                         unsigned flags, void *stream);
+
+/* ---- initial states, built on the device (W: 5*n^3 floats, n^3 grid) ---- */
+
+/* scaling_jax.py:23-41 setup_ics(n, k): rho = 0.125, p = 0.1, u = 0; rho = p = 1
+ * on [n/2-k, n/2+k)^3.  The caller uses dx = 1/(n-1) like the reference. */
+int tf_ics_injection_cube(float *W, int n, int num_injection_cells, void *stream);
+
+/* Spherical overpressure on the unit periodic cube (cell centres (i+0.5)/n):
+ * p = p_in for r < radius around the centre else p_out, u = 0,
+ * rho = rho0*(1 + noise*U(-1,1)) from a counter-based hash of seed.  No
+ * reference counterpart (benchmark initial state). */
+int tf_ics_overpressure(float *W, int n, unsigned long long seed, double radius, double p_in,
+                        double p_out, double rho0, double noise, void *stream);
+
+/* Shear layer: rho=2, vx=+0.5 for |y-0.5|<0.25, else rho=1, vx=-0.5; p=2.5;
+ * vy = amplitude*sin(4 pi x)*a with a ~ N(0,1) per cell (seeded hash); vz=0.
+ * No reference counterpart (benchmark initial state). */
+int tf_ics_shear_layer(float *W, int n, unsigned long long seed, double amplitude, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TINYFLUIDS_GB300_H */

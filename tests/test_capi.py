@@ -1,0 +1,92 @@
+"""The C-ABI library: builds, loads, exports every declared symbol, and
+rejects bad arguments on the host (CPU only: no compute calls)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))
+           if f.endswith(".h")]
+
+
+def declared_functions():
+    names = set()
+    for h in HEADERS:
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[a-z_ ]+\**\s*\**(tf_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from tinyfluids_gb300 import _lib, build
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_functions():
+    names = declared_functions()
+    assert "tf_evolve_state" in names and "tf_time_integration" in names
+    assert len(names) >= 10
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+
+
+def test_python_binding_covers_every_declared_symbol():
+    from tinyfluids_gb300 import _lib
+    assert set(declared_functions()) == set(_lib.SIGNATURES)
+
+
+def test_abi_and_status_strings(lib):
+    assert lib.tf_abi_version() == 1
+    assert lib.tf_ctl_bytes() == 64
+    assert lib.tf_status_string(0) == b"ok"
+    assert b"argument" in lib.tf_status_string(1)
+
+
+def test_host_side_argument_checks(lib):
+    """Bad arguments are rejected before any CUDA call, with a message."""
+    from tinyfluids_gb300 import _lib
+    with pytest.raises(_lib.TinyfluidsError) as e:
+        _lib.call("tf_evolve_state", None, None, 4, 4, 4, 0.1, 0.01, None, 5 / 3, 0, None, None)
+    assert e.value.status == 1
+    fake = ctypes.c_void_p(0x1000)
+    with pytest.raises(_lib.TinyfluidsError) as e:  # aliasing output
+        _lib.call("tf_evolve_state", fake, fake, 4, 4, 4, 0.1, 0.01, None, 5 / 3, 0, None, None)
+    assert "alias" in str(e.value)
+    other = ctypes.c_void_p(0x2000)
+    with pytest.raises(_lib.TinyfluidsError):  # zero-size axis
+        _lib.call("tf_evolve_state", fake, other, 0, 4, 4, 0.1, 0.01, None, 5 / 3, 0, None, None)
+    with pytest.raises(_lib.TinyfluidsError):  # open boundaries need 2 cells
+        _lib.call("tf_evolve_state", fake, other, 1, 4, 4, 0.1, 0.01, None, 5 / 3, 1, None, None)
+    with pytest.raises(_lib.TinyfluidsError):  # gamma == 1
+        _lib.call("tf_evolve_state", fake, other, 4, 4, 4, 0.1, 0.01, None, 1.0, 0, None, None)
+    with pytest.raises(_lib.TinyfluidsError):  # bad tile rows
+        tc = _lib.TileConfig(12, 4)
+        _lib.call("tf_evolve_state", fake, other, 4, 4, 4, 0.1, 0.01, None, 5 / 3, 0,
+                  ctypes.byref(tc), None)
+    with pytest.raises(_lib.TinyfluidsError):  # unbounded loop
+        _lib.call("tf_time_integration", fake, other, ctypes.c_void_p(0x3000),
+                  ctypes.c_void_p(0x4000), 4, 4, 4, 0.1, float("inf"), 5 / 3, 0.4, -1, 0.0, 0,
+                  None, None, None)
+
+
+def test_python_api_validates_before_launch():
+    import torch
+    import tinyfluids_gb300 as tg
+    with pytest.raises(TypeError):
+        tg._evolve_state(torch.zeros(4, 3, 3, 3), 0.1, 0.01, 5 / 3)
+    with pytest.raises(TypeError):
+        tg._evolve_state(torch.zeros(5, 3, 3, 3, dtype=torch.float64), 0.1, 0.01, 5 / 3)
+    with pytest.raises(ValueError):  # CPU tensors: no CPU path
+        tg._evolve_state(torch.zeros(5, 3, 3, 3), 0.1, 0.01, 5 / 3)
+    with pytest.raises(NotImplementedError):
+        tg.time_integration.time_integration(torch.zeros(5, 3, 3, 3), 0.1, 0.2, 5 / 3, False,
+                                             True)

@@ -1,0 +1,192 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle.
+
+Bar: the exact policy (TF_FLAG_EXACT, the reference's op order) is
+bit-identical to the float32 oracle; the fast policy agrees with it to
+FAST_STEP_RTOL per step (relative to each variable's max magnitude) and its
+density error against the FP64 oracle stays within 2x the reference float32
+scheme's own error.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import fluid_np as F
+from oracle import ics_np as I
+
+pytestmark = pytest.mark.gpu
+
+GAMMA = 5.0 / 3.0
+FAST_STEP_RTOL = 2e-6   # one fast step vs the float32 reference scheme
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                     "iteration_counts.json")))
+
+SHAPES = [(1, 1, 1), (2, 3, 5), (5, 7, 33), (16, 16, 16), (33, 17, 61), (40, 31, 64),
+          (3, 64, 29), (64, 15, 2)]
+
+
+def random_state(shape, seed):
+    rng = np.random.default_rng(seed)
+    W = np.empty((5,) + tuple(shape), np.float32)
+    W[0] = rng.uniform(0.5, 2.0, shape)
+    W[1:4] = rng.uniform(-1.0, 1.0, (3,) + tuple(shape))
+    W[4] = rng.uniform(0.2, 3.0, shape)
+    return W
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+def rel_err(a, b):
+    scale = np.abs(b).reshape(5, -1).max(axis=1).reshape(5, 1, 1, 1) + 1e-30
+    return float((np.abs(a - b) / scale).max())
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("hb", [False, True])
+def test_exact_fused_step_bit_identical(tg, shape, hb):
+    if hb and min(shape) < 2:
+        pytest.skip("open boundaries need two cells per axis")
+    W = random_state(shape, hash(shape) % 1000)
+    dx = 0.05
+    dt = F._cfl_time_step(W, dx, GAMMA)
+    ref = F._evolve_state(W, dx, dt, GAMMA, hb)
+    for tile in (None, (8, 3), (16, 1)):
+        out = host(tg._evolve_state(dev(W), dx, float(dt), GAMMA, hb, exact=True, tile=tile))
+        assert np.array_equal(out, ref), (shape, hb, tile, np.abs(out - ref).max())
+
+
+@pytest.mark.parametrize("shape", [(5, 7, 33), (16, 16, 16), (9, 1, 4)])
+@pytest.mark.parametrize("axis", [1, 2, 3])
+def test_exact_sweep_bit_identical(tg, shape, axis):
+    W = random_state(shape, 5)
+    dt = np.float32(0.003)
+    ref = F._evolve_state_along_axis(W, 0.05, dt, GAMMA, axis)
+    out = host(tg._evolve_state_along_axis(dev(W), 0.05, float(dt), GAMMA, axis, exact=True))
+    assert np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_cfl_time_step_bit_identical(tg, shape):
+    W = random_state(shape, 9)
+    ref = F._cfl_time_step(W, 0.02, GAMMA)
+    out = tg._cfl_time_step(dev(W), 0.02, GAMMA)
+    assert out.shape == () and out.dtype == torch.float32
+    assert float(out) == float(ref)
+
+
+def test_conversions_bit_identical(tg):
+    W = random_state((7, 9, 11), 2)
+    U = F.conserved_state_from_primitive(W, GAMMA)
+    assert np.array_equal(host(tg.conserved_state_from_primitive(dev(W), GAMMA)), U)
+    assert np.array_equal(host(tg.primitive_state_from_conserved(dev(U), GAMMA)),
+                          F.primitive_state_from_conserved(U, GAMMA))
+
+
+def test_dt_from_device_tensor(tg):
+    W = random_state((12, 10, 8), 4)
+    dt = tg._cfl_time_step(dev(W), 0.05, GAMMA)
+    a = host(tg._evolve_state(dev(W), 0.05, dt, GAMMA, exact=True))
+    b = F._evolve_state(W, 0.05, F._cfl_time_step(W, 0.05, GAMMA), GAMMA)
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("n", [32, 64, 96, 128, 196, 256])
+def test_exact_time_integration_reproduces_reference_counts(tg, oracle_lib, n):
+    """The reference's golden data: steps to t=0.2 for setup_ics(n, n//16)."""
+    W, dx = tg.setup_ics(n, n // 16)
+    Wf, it = tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False, exact=True)
+    assert int(it) == GOLDEN["counts"][str(n)]
+    if n <= 64:
+        ref, rit = oracle_lib.time_integration(host(W), dx, 0.2, GAMMA, True)
+        assert rit == int(it)
+        assert np.array_equal(host(Wf), ref)
+
+
+@pytest.mark.parametrize("n", [32, 64, 96, 128])
+def test_fast_time_integration_reproduces_reference_counts(tg, n):
+    W, dx = tg.setup_ics(n, n // 16)
+    _, it = tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False)
+    assert int(it) == GOLDEN["counts"][str(n)]
+
+
+def test_setup_ics_matches_reference_builder(tg):
+    W, dx = tg.setup_ics(40, 40 // 16)
+    Wn, dxn = I.setup_ics(40, 40 // 16)
+    assert dx == dxn and np.array_equal(host(W), Wn)
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("hb", [False, True])
+def test_fast_step_close_to_reference(tg, shape, hb):
+    if hb and min(shape) < 2:
+        pytest.skip("open boundaries need two cells per axis")
+    W = random_state(shape, 21)
+    dt = F._cfl_time_step(W, 0.05, GAMMA)
+    ref = F._evolve_state(W, 0.05, dt, GAMMA, hb)
+    out = host(tg._evolve_state(dev(W), 0.05, float(dt), GAMMA, hb))
+    assert rel_err(out, ref) < FAST_STEP_RTOL
+
+
+def test_fast_step_independent_of_tile_shape(tg):
+    W = dev(random_state((70, 45, 77), 8))
+    outs = [host(tg._evolve_state(W, 0.05, 1e-3, GAMMA, tile=t))
+            for t in (None, (16, 64), (16, 5), (8, 1), (8, 70))]
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+
+
+@pytest.mark.parametrize("axis,shift", [(1, 3), (2, -5), (3, 31)])
+def test_fast_step_roll_equivariant(tg, axis, shift):
+    W = random_state((40, 36, 70), 12)
+    a = host(tg._evolve_state(dev(np.roll(W, shift, axis)), 0.05, 2e-3, GAMMA))
+    b = np.roll(host(tg._evolve_state(dev(W), 0.05, 2e-3, GAMMA)), shift, axis)
+    assert np.array_equal(a, b)
+
+
+def test_fast_run_conserves_totals(tg):
+    W, dx = tg.overpressure(48, seed=5)
+    U0 = F.conserved_state_from_primitive(host(W).astype(np.float64), GAMMA).sum(axis=(1, 2, 3))
+    Wf = tg.run_steps(W, dx, GAMMA, 20)
+    U1 = F.conserved_state_from_primitive(host(Wf).astype(np.float64), GAMMA).sum(axis=(1, 2, 3))
+    assert np.allclose(U0, U1, rtol=2e-5, atol=1e-3)
+
+
+def test_overpressure_64_accuracy_vs_fp64(tg, oracle_lib):
+    """Config 1: 64^3 overpressure, CFL 0.4, 100 steps.  The fast path's density
+    error against the FP64 oracle is within 2x the reference float32 scheme's."""
+    W, dx = tg.overpressure(64, seed=0)
+    W0 = host(W)
+    ref32, dts32 = oracle_lib.run_steps(W0, dx, GAMMA, 100)
+    ref64, _ = oracle_lib.run_steps(W0.astype(np.float64), dx, GAMMA, 100)
+    fast = host(tg.run_steps(W, dx, GAMMA, 100))
+    exact = host(tg.run_steps(W, dx, GAMMA, 100, exact=True))
+    assert np.array_equal(exact, ref32)
+    e_ref_l1 = np.abs(ref32[0] - ref64[0]).mean()
+    e_ref_inf = np.abs(ref32[0] - ref64[0]).max()
+    e_fast_l1 = np.abs(fast[0] - ref64[0]).mean()
+    e_fast_inf = np.abs(fast[0] - ref64[0]).max()
+    print(f"density error vs FP64: reference-f32 L1 {e_ref_l1:.3e} Linf {e_ref_inf:.3e}; "
+          f"fast L1 {e_fast_l1:.3e} Linf {e_fast_inf:.3e}")
+    assert e_fast_l1 <= 2 * e_ref_l1 and e_fast_inf <= 2 * e_ref_inf
+
+
+def test_nonfinite_state_is_reported(tg):
+    W = random_state((8, 8, 8), 1)
+    W[4, 3, 3, 3] = -1.0  # negative pressure: sound speed is NaN
+    with pytest.raises(tg.TinyfluidsError) as e:
+        tg.time_integration_fn(dev(W), 0.1, 0.5, GAMMA, False, False)
+    assert e.value.status == 3
+
+
+def test_time_integration_zero_and_negative_t_final(tg):
+    W = dev(random_state((6, 6, 6), 3))
+    Wf, it = tg.time_integration_fn(W, 0.1, 0.0, GAMMA, False, False)
+    assert int(it) == 0 and torch.equal(Wf, W)

@@ -1,0 +1,100 @@
+"""ctypes binding of the C-ABI library ``_lib/libtinyfluids_gb300.so``.
+
+The library is the only compute path of this package: there is no CPU or
+PyTorch fallback.  If it is missing, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_LOCK = threading.Lock()
+_LIB = None
+
+c_int = ctypes.c_int
+c_uint = ctypes.c_uint
+c_float = ctypes.c_float
+c_ll = ctypes.c_longlong
+c_ull = ctypes.c_ulonglong
+vp = ctypes.c_void_p
+c_char_p = ctypes.c_char_p
+
+
+class TileConfig(ctypes.Structure):
+    """tf_tile_config: warps per CTA (8 or 16, incl. 2 halo rows) and x planes per CTA."""
+    _fields_ = [("rows", c_int), ("lx", c_int)]
+
+
+# name -> (restype, argtypes); mirrors include/tinyfluids_gb300.h
+SIGNATURES = {
+    "tf_abi_version": (c_int, []),
+    "tf_status_string": (c_char_p, [c_int]),
+    "tf_last_error": (c_char_p, []),
+    "tf_ctl_bytes": (c_ull, []),
+    "tf_conserved_from_primitive": (c_int, [vp, vp, c_ll, c_float, vp]),
+    "tf_primitive_from_conserved": (c_int, [vp, vp, c_ll, c_float, vp]),
+    "tf_cfl_time_step": (c_int, [vp, c_int, c_int, c_int, c_float, c_float, c_float, vp, vp]),
+    "tf_evolve_state": (c_int, [vp, vp, c_int, c_int, c_int, c_float, c_float, vp, c_float,
+                                c_uint, vp, vp]),
+    "tf_time_integration": (c_int, [vp, vp, vp, vp, c_int, c_int, c_int, c_float, c_float,
+                                    c_float, c_float, c_int, c_float, c_uint, vp, vp, vp]),
+    "tf_evolve_along_axis": (c_int, [vp, vp, c_int, c_int, c_int, c_float, c_float, vp,
+                                     c_float, c_int, c_uint, vp]),
+    "tf_ics_injection_cube": (c_int, [vp, c_int, c_int, vp]),
+    "tf_ics_overpressure": (c_int, [vp, c_int, c_ull, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]),
+    "tf_ics_shear_layer": (c_int, [vp, c_int, c_ull, ctypes.c_double, vp]),
+}
+
+TF_OK = 0
+TF_FLAG_OPEN_BOUNDARIES = 1
+TF_FLAG_EXACT = 2
+
+
+class TinyfluidsError(RuntimeError):
+    """A C-ABI call returned a non-zero tf_status."""
+
+    def __init__(self, status, message):
+        super().__init__(message)
+        self.status = status
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load():
+    """Load (once) and return the C-ABI library; raises if it was not built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = _build.LIB
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"tinyfluids_gb300 CUDA library not found at {path}; build it with "
+                "`python -m tinyfluids_gb300.build` (nvcc, sm_103a). There is no CPU fallback.")
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        if L.tf_abi_version() != 1:
+            raise RuntimeError("tinyfluids_gb300 library ABI mismatch")
+        _LIB = L
+    return _LIB
+
+
+def call(name, *args):
+    """Call a C-ABI function and raise TinyfluidsError on a non-zero status."""
+    L = load()
+    st = getattr(L, name)(*args)
+    if st != TF_OK:
+        msg = L.tf_last_error().decode(errors="replace")
+        raise TinyfluidsError(st, f"{name}: {L.tf_status_string(st).decode()}: {msg}")
+    return st

@@ -1,0 +1,526 @@
+// Single-instance kernels and their C ABI: conversions, the CFL dt, the
+// fused step, the per-axis sweep and the run-to-time loop.
+#include <math.h>
+#include <string.h>
+
+#include <mutex>
+#include <vector>
+
+#include "tf_common.cuh"
+#include "tf_fused.cuh"
+#include "tf_host.h"
+#include "tf_math.cuh"
+
+namespace tf {
+
+// ---------------------------------------------------------------------------
+// error reporting
+// ---------------------------------------------------------------------------
+static thread_local char g_err[512] = "";
+
+int set_error(int status, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  return status;
+}
+
+int sm_count() {
+  static std::mutex mu;
+  static std::vector<int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+  if (cache[dev] == 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 148;
+    cache[dev] = n;
+  }
+  return cache[dev];
+}
+
+template <typename T>
+static StepConsts<T> make_consts(T gamma, T dx, T dt) {
+  StepConsts<T> k;
+  k.g = gamma;
+  k.gm1 = gamma - T(1);
+  k.igm1 = T(1) / k.gm1;
+  k.inv_dx = T(1) / dx;
+  k.dt = dt;
+  k.k = dt * k.inv_dx;
+  return k;
+}
+
+// ---------------------------------------------------------------------------
+// conversions (fluid.py:30-103), exact arithmetic
+// ---------------------------------------------------------------------------
+__global__ void cons_from_prim_kernel(const float* __restrict__ W, float* __restrict__ U,
+                                      long long n, StepConsts<float> k) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float w[5], u[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) w[v] = W[v * n + i];
+    exact_cons_from_prim(w, u, k);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) U[v * n + i] = u[v];
+  }
+}
+
+__global__ void prim_from_cons_kernel(const float* __restrict__ U, float* __restrict__ W,
+                                      long long n, StepConsts<float> k) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float u[5], w[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) u[v] = U[v * n + i];
+    exact_prim_from_cons(u, w, k);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) W[v * n + i] = w[v];
+  }
+}
+
+static int elementwise_grid(long long n) {
+  long long b = (n + 255) / 256;
+  long long cap = (long long)sm_count() * 8;
+  return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
+}
+
+// ---------------------------------------------------------------------------
+// control block
+// ---------------------------------------------------------------------------
+__global__ void ctl_init_kernel(tf_ctl* ctl, float t_final, float cfl_dx, int max_steps) {
+  ctl->t = 0.f;
+  ctl->dt = 0.f;
+  ctl->t_final = t_final;
+  ctl->cfl_dx = cfl_dx;
+  ctl->ws_bits = 0u;
+  ctl->done = 0u;
+  ctl->iter = 0;
+  ctl->active = 0;
+  ctl->max_steps = max_steps;
+  ctl->status = TF_OK;
+  ctl->max_speed = 0.f;
+}
+
+// Max wave speed of a primitive state (fluid.py:427-500 in per-cell form);
+// the last CTA sets ctl->dt and the loop condition.
+__global__ void __launch_bounds__(256) maxspeed_kernel(const float* __restrict__ W, long long n,
+                                                       float g, tf_ctl* ctl) {
+  __shared__ float red[8];
+  float m = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float w[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) w[v] = __ldg(W + v * n + i);
+    m = speed_max(m, exact_cell_speed(w, g));
+  }
+  float bm = block_max(m, red);
+  if (threadIdx.x == 0) ctl_finish_cta(ctl, bm, gridDim.x, 0.f, false);
+}
+
+// Copies the final state of a loop into `out` unless it already is there.
+// After `iter` steps the state is in src0 (iter == 0) or buf[iter & 1].
+__global__ void final_select_kernel(const tf_ctl* ctl, const float* __restrict__ src0,
+                                    const float* buf0, const float* buf1, float* out,
+                                    long long n) {
+  int iter = ld_volatile(&ctl->iter);
+  const float* from = iter == 0 ? src0 : ((iter & 1) ? buf1 : buf0);
+  if (from == out) return;
+  const float4* f4 = reinterpret_cast<const float4*>(from);
+  float4* o4 = reinterpret_cast<float4*>(out);
+  long long n4 = n / 4;
+  long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long st = (long long)gridDim.x * blockDim.x;
+  bool vec = ((reinterpret_cast<uintptr_t>(from) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+  if (vec) {
+    for (long long i = i0; i < n4; i += st) o4[i] = f4[i];
+    for (long long i = n4 * 4 + i0; i < n; i += st) out[i] = from[i];
+  } else {
+    for (long long i = i0; i < n; i += st) out[i] = from[i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fused step
+// ---------------------------------------------------------------------------
+struct FusedArgs {
+  const float* src0;  // input state (iteration 0 in loop mode)
+  float* buf[2];      // fixed mode: buf[1] = output; loop mode: ping-pong
+  FusedGeom geo;
+  float gamma, inv_dx, gm1, igm1;
+  float dt_host;
+  const float* dt_dev;
+  float fixed_dt;  // loop mode: > 0 replaces ctl->dt
+  tf_ctl* ctl;     // fixed mode: optional; loop mode: required
+  int loop;        // 1: predicated loop step (parity buffers, dt from ctl)
+};
+
+template <class P, int NW>
+__global__ void __launch_bounds__(NW * 32, 1) fused_step_kernel(FusedArgs a) {
+  __shared__ FusedSmem<NW> sm;
+  const float* src;
+  float* dst;
+  float dt;
+  if (a.loop) {
+    if (!ld_volatile(&a.ctl->active)) return;
+    int iter = ld_volatile(&a.ctl->iter);
+    src = iter == 0 ? a.src0 : ((iter & 1) ? a.buf[1] : a.buf[0]);
+    dst = (iter & 1) ? a.buf[0] : a.buf[1];
+    dt = a.fixed_dt > 0.f ? a.fixed_dt : ld_volatile(&a.ctl->dt);
+  } else {
+    src = a.src0;
+    dst = a.buf[1];
+    dt = a.dt_dev ? *a.dt_dev : a.dt_host;
+  }
+  StepConsts<float> K;
+  K.g = a.gamma;
+  K.gm1 = a.gm1;
+  K.igm1 = a.igm1;
+  K.inv_dx = a.inv_dx;
+  K.dt = dt;
+  K.k = dt * a.inv_dx;
+  float m = fused_tile<P, NW>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z, K, sm);
+  if (a.ctl) {
+    float bm = block_max(m, sm.red);
+    if (threadIdx.x == 0)
+      ctl_finish_cta(a.ctl, bm, gridDim.x * gridDim.y * gridDim.z, dt, a.loop != 0);
+  }
+}
+
+static int check_dims(int nx, int ny, int nz, unsigned flags) {
+  if (nx < 1 || ny < 1 || nz < 1)
+    return set_error(TF_ERR_ARG, "grid dims must be >= 1 (got %d,%d,%d)", nx, ny, nz);
+  if ((flags & TF_FLAG_OPEN_BOUNDARIES) && (nx < 2 || ny < 2 || nz < 2))
+    return set_error(TF_ERR_ARG, "open boundaries need >= 2 cells per axis (fluid.py:349,374)");
+  if ((long long)nx * ny * nz > (1LL << 40))
+    return set_error(TF_ERR_ARG, "grid too large");
+  return TF_OK;
+}
+
+static int check_scalars(float dx, float gamma) {
+  if (!(dx > 0.f) || !isfinite(dx)) return set_error(TF_ERR_ARG, "dx must be finite and > 0");
+  if (!isfinite(gamma) || gamma == 1.f) return set_error(TF_ERR_ARG, "gamma must be finite and != 1");
+  return TF_OK;
+}
+
+static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int lx) {
+  FusedGeom g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nz = nz;
+  g.open_bc = (flags & TF_FLAG_OPEN_BOUNDARIES) ? 1 : 0;
+  g.tiles_z = (nz + kTileZ - 1) / kTileZ;
+  g.tiles_y = (ny + (rows - 2) - 1) / (rows - 2);
+  if (lx <= 0) {
+    // enough CTAs for ~8 waves at one CTA per SM, chunks of >= 8 planes
+    long long tiles_yz = (long long)g.tiles_z * g.tiles_y;
+    long long want = 8LL * sm_count();
+    long long tx = (want + tiles_yz - 1) / tiles_yz;
+    long long max_tx = nx / 8 > 0 ? nx / 8 : 1;
+    if (tx > max_tx) tx = max_tx;
+    if (tx < 1) tx = 1;
+    lx = (int)((nx + tx - 1) / tx);
+  }
+  if (lx > nx) lx = nx;
+  g.lx = lx;
+  g.tiles_x = (nx + lx - 1) / lx;
+  return g;
+}
+
+static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx) {
+  *rows = 16;
+  *lx = 0;
+  if (tile) {
+    if (tile->rows != 8 && tile->rows != 16)
+      return set_error(TF_ERR_ARG, "tile rows must be 8 or 16 (got %d)", tile->rows);
+    *rows = tile->rows;
+    *lx = tile->lx;
+    if (*lx < 0) return set_error(TF_ERR_ARG, "tile lx must be >= 0");
+  }
+  return TF_OK;
+}
+
+static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s) {
+  if (a.geo.tiles_y > 65535 || a.geo.tiles_x > 65535)
+    return set_error(TF_ERR_ARG, "grid too large for the tile grid");
+  dim3 grid(a.geo.tiles_z, a.geo.tiles_y, a.geo.tiles_x);
+  if (exact) {
+    if (rows == 16) fused_step_kernel<ExactPolicy<float>, 16><<<grid, 16 * 32, 0, s>>>(a);
+    else fused_step_kernel<ExactPolicy<float>, 8><<<grid, 8 * 32, 0, s>>>(a);
+  } else {
+    if (rows == 16) fused_step_kernel<FastPolicy, 16><<<grid, 16 * 32, 0, s>>>(a);
+    else fused_step_kernel<FastPolicy, 8><<<grid, 8 * 32, 0, s>>>(a);
+  }
+  return launch_check("fused_step_kernel");
+}
+
+static FusedArgs make_fused_args(const float* src, float* b0, float* b1, const FusedGeom& geo,
+                                 float dx, float gamma) {
+  FusedArgs a;
+  memset(&a, 0, sizeof a);
+  a.src0 = src;
+  a.buf[0] = b0;
+  a.buf[1] = b1;
+  a.geo = geo;
+  StepConsts<float> k = make_consts<float>(gamma, dx, 0.f);
+  a.gamma = k.g;
+  a.gm1 = k.gm1;
+  a.igm1 = k.igm1;
+  a.inv_dx = k.inv_dx;
+  return a;
+}
+
+// ---------------------------------------------------------------------------
+// per-axis sweep (one thread per cell, both faces recomputed): the
+// reference's structure, used to cross-check the fused kernel and by the
+// adjoint's forward recomputation.
+// ---------------------------------------------------------------------------
+template <class P, int VEL>
+__global__ void __launch_bounds__(256) sweep_kernel(const float* __restrict__ src,
+                                                    float* __restrict__ dst, int nx, int ny,
+                                                    int nz, int open_bc, int in_prim,
+                                                    int out_prim, StepConsts<float> K) {
+  const long long n = (long long)nx * ny * nz;
+  const bool open = open_bc != 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    int z = (int)(i % nz);
+    long long r = i / nz;
+    int y = (int)(r % ny);
+    int x = (int)(r / ny);
+    Cell<float> c[3];
+#pragma unroll
+    for (int d = -1; d <= 1; ++d) {
+      int xx = x, yy = y, zz = z;
+      if (VEL == 1) xx += d;
+      if (VEL == 2) yy += d;
+      if (VEL == 3) zz += d;
+      long long j = ((long long)src_index(xx, nx, open) * ny + src_index(yy, ny, open)) * nz +
+                    src_index(zz, nz, open);
+      float w[5], s[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) w[v] = __ldg(src + v * n + j);
+      if (in_prim) P::to_state(w, s, K);
+      else {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) s[v] = w[v];
+      }
+      P::template derive<VEL>(s, c[d + 1], K);
+    }
+    float flo[5], fhi[5], s[5], o[5];
+    P::hll(c[0], c[1], flo);
+    P::hll(c[1], c[2], fhi);
+    P::update(c[1], flo, fhi, s, K);
+    if (out_prim) P::to_prim(s, o, K);
+    else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) o[v] = s[v];
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) dst[v * n + i] = o[v];
+  }
+}
+
+}  // namespace tf
+
+using namespace tf;
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int tf_abi_version(void) { return TF_ABI_VERSION; }
+
+const char* tf_status_string(int status) {
+  switch (status) {
+    case TF_OK: return "ok";
+    case TF_ERR_ARG: return "invalid argument";
+    case TF_ERR_CUDA: return "CUDA error";
+    case TF_ERR_NONFINITE: return "non-finite or zero max wave speed";
+    case TF_ERR_TIMEOUT: return "device-side wait timed out";
+    case TF_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+const char* tf_last_error(void) { return g_err; }
+
+unsigned long long tf_ctl_bytes(void) { return sizeof(tf_ctl); }
+
+int tf_conserved_from_primitive(const float* W, float* U, long long ncells, float gamma,
+                                void* stream) {
+  if (!W || !U || ncells < 0) return set_error(TF_ERR_ARG, "bad arguments");
+  if (W == U) return set_error(TF_ERR_ARG, "output must not alias input");
+  if (ncells == 0) return TF_OK;
+  StepConsts<float> k = make_consts<float>(gamma, 1.f, 0.f);
+  cons_from_prim_kernel<<<elementwise_grid(ncells), 256, 0, (cudaStream_t)stream>>>(W, U, ncells, k);
+  return launch_check("cons_from_prim_kernel");
+}
+
+int tf_primitive_from_conserved(const float* U, float* W, long long ncells, float gamma,
+                                void* stream) {
+  if (!W || !U || ncells < 0) return set_error(TF_ERR_ARG, "bad arguments");
+  if (W == U) return set_error(TF_ERR_ARG, "output must not alias input");
+  if (ncells == 0) return TF_OK;
+  StepConsts<float> k = make_consts<float>(gamma, 1.f, 0.f);
+  prim_from_cons_kernel<<<elementwise_grid(ncells), 256, 0, (cudaStream_t)stream>>>(U, W, ncells, k);
+  return launch_check("prim_from_cons_kernel");
+}
+
+int tf_cfl_time_step(const float* W, int nx, int ny, int nz, float dx, float gamma, float cfl,
+                     tf_ctl* ctl, void* stream) {
+  if (!W || !ctl) return set_error(TF_ERR_ARG, "null pointer");
+  TF_TRY(check_dims(nx, ny, nz, 0));
+  TF_TRY(check_scalars(dx, gamma));
+  if (!(cfl > 0.f) || !isfinite(cfl)) return set_error(TF_ERR_ARG, "C_CFL must be finite and > 0");
+  cudaStream_t s = (cudaStream_t)stream;
+  long long n = (long long)nx * ny * nz;
+  float cfl_dx = cfl * dx;  // fluid.py:502, rounded to float like the traced product
+  ctl_init_kernel<<<1, 1, 0, s>>>(ctl, 0.f, cfl_dx, 0);
+  maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W, n, gamma, ctl);
+  return launch_check("maxspeed_kernel");
+}
+
+int tf_evolve_state(const float* W_in, float* W_out, int nx, int ny, int nz, float dx,
+                    float dt_host, const float* dt_dev, float gamma, unsigned flags,
+                    const tf_tile_config* tile, void* stream) {
+  if (!W_in || !W_out) return set_error(TF_ERR_ARG, "null state pointer");
+  if (W_in == W_out) return set_error(TF_ERR_ARG, "W_out must not alias W_in");
+  TF_TRY(check_dims(nx, ny, nz, flags));
+  TF_TRY(check_scalars(dx, gamma));
+  if (!dt_dev && !isfinite(dt_host)) return set_error(TF_ERR_ARG, "dt must be finite");
+  int rows, lx;
+  TF_TRY(resolve_tile(tile, &rows, &lx));
+  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
+  FusedArgs a = make_fused_args(W_in, nullptr, W_out, geo, dx, gamma);
+  a.dt_host = dt_host;
+  a.dt_dev = dt_dev;
+  a.loop = 0;
+  a.ctl = nullptr;
+  return launch_fused(a, rows, (flags & TF_FLAG_EXACT) != 0, (cudaStream_t)stream);
+}
+
+int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ctl, int nx, int ny,
+                        int nz, float dx, float t_final, float gamma, float cfl, int max_steps,
+                        float fixed_dt, unsigned flags, const tf_tile_config* tile,
+                        int* iters_host, void* stream) {
+  if (!W_in || !W_out || !work || !ctl) return set_error(TF_ERR_ARG, "null pointer");
+  if (W_in == W_out || W_in == work || W_out == work)
+    return set_error(TF_ERR_ARG, "W_in, W_out and work must be distinct buffers");
+  TF_TRY(check_dims(nx, ny, nz, flags));
+  TF_TRY(check_scalars(dx, gamma));
+  if (!(cfl > 0.f) || !isfinite(cfl)) return set_error(TF_ERR_ARG, "C_CFL must be finite and > 0");
+  if (isnan(t_final)) return set_error(TF_ERR_ARG, "t_final is NaN");
+  if (!(fixed_dt >= 0.f) || !isfinite(fixed_dt)) return set_error(TF_ERR_ARG, "fixed_dt must be >= 0");
+  if (max_steps < 0 && !isfinite(t_final))
+    return set_error(TF_ERR_ARG, "an unbounded loop needs a finite t_final or max_steps >= 0");
+  int rows, lx;
+  TF_TRY(resolve_tile(tile, &rows, &lx));
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long n = (long long)nx * ny * nz;
+  const bool exact = (flags & TF_FLAG_EXACT) != 0;
+
+  ctl_init_kernel<<<1, 1, 0, s>>>(ctl, t_final, cfl * dx, max_steps);
+  maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W_in, n, gamma, ctl);
+  TF_TRY(launch_check("maxspeed_kernel"));
+
+  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
+  // with a known step count, choose the ping-pong roles so that the last
+  // step writes W_out (step i writes buf[i & 1], i = 1..max_steps)
+  float* b0 = work;
+  float* b1 = W_out;
+  if (max_steps >= 0 && (max_steps & 1) == 0) {
+    b0 = W_out;
+    b1 = work;
+  }
+  FusedArgs a = make_fused_args(W_in, b0, b1, geo, dx, gamma);
+  a.loop = 1;
+  a.ctl = ctl;
+  a.fixed_dt = fixed_dt;
+
+  if (max_steps >= 0) {
+    // step count known: enqueue exactly that many predicated steps
+    for (int i = 0; i < max_steps; ++i) TF_TRY(launch_fused(a, rows, exact, s));
+  } else {
+    // run to t_final: chunks of predicated steps, one host check per chunk
+    static thread_local tf_ctl* pinned = nullptr;
+    if (!pinned) TF_TRY(cuda_check(cudaMallocHost(&pinned, sizeof(tf_ctl)), "cudaMallocHost"));
+    int chunk = 8;
+    long long launched = 0;
+    float t_prev = -1.f;
+    for (;;) {
+      for (int i = 0; i < chunk; ++i) TF_TRY(launch_fused(a, rows, exact, s));
+      launched += chunk;
+      TF_TRY(cuda_check(cudaMemcpyAsync(pinned, ctl, sizeof(tf_ctl), cudaMemcpyDeviceToHost, s),
+                        "cudaMemcpyAsync(ctl)"));
+      TF_TRY(cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
+      if (!pinned->active) break;
+      // float32 t no longer advances (t + dt == t): the reference would loop
+      // forever here; report it instead
+      if (pinned->t == t_prev)
+        return set_error(TF_ERR_NONFINITE, "time stalled at t=%g (dt=%g below float spacing)",
+                         (double)pinned->t, (double)pinned->dt);
+      t_prev = pinned->t;
+      if (launched > (1LL << 28)) return set_error(TF_ERR_ARG, "loop did not terminate");
+      // remaining steps at the current dt, with margin; predicated steps past
+      // the end cost only a launch
+      double rem = pinned->dt > 0.f ? ((double)t_final - pinned->t) / pinned->dt : 8.0;
+      double want = rem * 1.1 + 2.0;
+      chunk = want < 4 ? 4 : (want > 512 ? 512 : (int)want);
+    }
+  }
+  final_select_kernel<<<elementwise_grid(5 * n / 4 + 1), 256, 0, s>>>(ctl, W_in, b0, b1, W_out,
+                                                                       5 * n);
+  TF_TRY(launch_check("final_select_kernel"));
+  if (iters_host) {
+    tf_ctl h;
+    TF_TRY(cuda_check(cudaMemcpyAsync(&h, ctl, sizeof(tf_ctl), cudaMemcpyDeviceToHost, s),
+                      "cudaMemcpyAsync(ctl)"));
+    TF_TRY(cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
+    *iters_host = h.iter;
+    if (h.status != TF_OK)
+      return set_error(h.status, "device reported %s after %d steps", tf_status_string(h.status),
+                       h.iter);
+  }
+  return TF_OK;
+}
+
+int tf_evolve_along_axis(const float* W_in, float* W_out, int nx, int ny, int nz, float dx,
+                         float dt_host, const float* dt_dev, float gamma, int axis, unsigned flags,
+                         void* stream) {
+  if (!W_in || !W_out) return set_error(TF_ERR_ARG, "null state pointer");
+  if (W_in == W_out) return set_error(TF_ERR_ARG, "W_out must not alias W_in");
+  if (axis < 0 || axis > 2) return set_error(TF_ERR_ARG, "axis must be 0, 1 or 2");
+  TF_TRY(check_dims(nx, ny, nz, flags));
+  TF_TRY(check_scalars(dx, gamma));
+  if (dt_dev) {
+    float h = 0.f;
+    TF_TRY(cuda_check(cudaMemcpyAsync(&h, dt_dev, sizeof(float), cudaMemcpyDeviceToHost,
+                                      (cudaStream_t)stream), "cudaMemcpyAsync(dt)"));
+    TF_TRY(cuda_check(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize"));
+    dt_host = h;
+  }
+  StepConsts<float> K = make_consts<float>(gamma, dx, dt_host);
+  long long n = (long long)nx * ny * nz;
+  int open = (flags & TF_FLAG_OPEN_BOUNDARIES) ? 1 : 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  int grid = elementwise_grid(n);
+  if (flags & TF_FLAG_EXACT) {
+    if (axis == 0) sweep_kernel<ExactPolicy<float>, 1><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
+    if (axis == 1) sweep_kernel<ExactPolicy<float>, 2><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
+    if (axis == 2) sweep_kernel<ExactPolicy<float>, 3><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
+  } else {
+    if (axis == 0) sweep_kernel<FastPolicy, 1><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
+    if (axis == 1) sweep_kernel<FastPolicy, 2><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
+    if (axis == 2) sweep_kernel<FastPolicy, 3><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
+  }
+  return launch_check("sweep_kernel");
+}
+
+}  // extern "C"

@@ -1,0 +1,74 @@
+"""Drop-in for ``tinyfluids.jax_tinyfluids.time_integration`` on a GB300.
+
+``time_integration`` keeps the reference's signature and loop semantics
+(time_integration.py:35-128): ``while t < t_final: dt = CFL dt(W);
+W = evolve(W, dt); t += dt; num_iterations += 1``, with ``t`` accumulated in
+float32 and the last step not clamped.  The loop runs on the device: each
+step is one fused kernel that also produces the next dt, and steps past the
+end are predicated off, so the host checks the condition only once per chunk
+of steps.
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+
+from . import _lib
+from .fluid import (CTL_ITER, CTL_STATUS, CTL_T, _flags, _scalar, _stream, _tile_arg,
+                    check_state, new_ctl)
+
+
+def time_integration(primitive_state, grid_spacing, t_final, gamma, handle_boundaries,
+                     shard_mapped, padding=None, split=None, *, C_CFL=0.4, exact=None,
+                     tile=None):
+    """time_integration.py:94-128.  Returns ``(state, num_iterations)``;
+    ``num_iterations`` is a 0-d int32 CUDA tensor like the reference's traced
+    counter.  ``shard_mapped=True`` (the multi-GPU shard_map branch) is out of
+    scope and raises."""
+    if shard_mapped or padding is not None or split is not None:
+        raise NotImplementedError(
+            "the shard_map branch (shard_mapped/padding/split) is not part of this "
+            "single-GPU implementation")
+    W, _, ctl = _run(primitive_state, grid_spacing, gamma, float(t_final), -1, 0.0,
+                     handle_boundaries, C_CFL, exact, tile, wait=True)
+    return W, ctl[CTL_ITER].clone()
+
+
+def run_steps(primitive_state, grid_spacing, gamma, num_steps, handle_boundaries=False, *,
+              C_CFL=0.4, dt=None, exact=None, tile=None, return_ctl=False):
+    """``num_steps`` iterations of the same loop body (CFL dt, or a fixed ``dt``),
+    fully asynchronous: nothing waits for the device.  Returns the state (and
+    the control block tensor with t, dt, iter, status when ``return_ctl``)."""
+    if int(num_steps) < 0:
+        raise ValueError("num_steps must be >= 0")
+    fixed = 0.0 if dt is None else float(dt)
+    if dt is not None and not (fixed > 0 and math.isfinite(fixed)):
+        raise ValueError("a fixed dt must be finite and > 0")
+    W, _, ctl = _run(primitive_state, grid_spacing, gamma, math.inf, int(num_steps), fixed,
+                     handle_boundaries, C_CFL, exact, tile, wait=False)
+    return (W, ctl) if return_ctl else W
+
+
+def _run(primitive_state, grid_spacing, gamma, t_final, max_steps, fixed_dt,
+         handle_boundaries, C_CFL, exact, tile, wait):
+    W = check_state(primitive_state)
+    _, nx, ny, nz = W.shape
+    with torch.cuda.device(W.device):
+        out = torch.empty_like(W)
+        work = torch.empty_like(W)
+        ctl = new_ctl(W.device)
+        it = _lib.ctypes.c_int(0)
+        _lib.call("tf_time_integration", W.data_ptr(), out.data_ptr(), work.data_ptr(),
+                  ctl.data_ptr(), nx, ny, nz, float(grid_spacing), float(t_final),
+                  _scalar(gamma, "gamma"), _scalar(C_CFL, "C_CFL"), int(max_steps),
+                  float(fixed_dt), _flags(handle_boundaries, exact), _tile_arg(tile),
+                  _lib.ctypes.byref(it) if wait else None, _stream(W))
+    return out, (it.value if wait else None), ctl
+
+
+def ctl_summary(ctl: torch.Tensor) -> dict:
+    """Host copy of a control block: t, iter, status (synchronises)."""
+    h = ctl.cpu()
+    return {"t": float(h.view(torch.float32)[CTL_T]), "iter": int(h[CTL_ITER]),
+            "status": int(h[CTL_STATUS])}
