@@ -68,9 +68,12 @@ def init_dist(world, backend):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms.
 
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Started before the warm-up so that nvidia-smi's own start-up never overlaps
+    the timed region; only samples inside [mark_start, mark_stop] are kept."""
+
+    QUERY = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -78,8 +81,9 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
 
-    def start(self):
+    def start(self, wait_s=15.0):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
@@ -89,35 +93,47 @@ class ClockSampler:
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
-        time.sleep(0.3)
+            return
+        end = time.time() + wait_s
+        while time.time() < end and os.path.getsize(self.path) == 0:
+            time.sleep(0.05)
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_stop(self):
+        self.t1 = time.time() + 0.25
 
     def stop(self):
         if self.proc is None:
             return None
+        time.sleep(0.3)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
         rows = []
+        from datetime import datetime
         for line in open(self.path):
             parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+                ts = datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(parts[2]), float(parts[3]), parts[6:10]))
             except ValueError:
                 continue
         os.unlink(self.path)
         if not rows:
             return None
-        load = [r for r in rows if r[0] > 0.5 * r[1]] or rows
+        win = [r for r in rows if self.t0 is None or (self.t0 <= r[0] <= self.t1)] or rows[-3:]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in load for i, v in enumerate(r[2])
+        reasons = sorted({names[i] for r in win for i, v in enumerate(r[3])
                           if v.lower() == "active"})
-        return {"sm_mhz": statistics.median(r[0] for r in load),
-                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
-                "samples": len(rows)}
+        return {"sm_mhz": statistics.median(r[1] for r in win),
+                "sm_max_mhz": max(r[2] for r in rows), "reasons": reasons,
+                "samples": len(win)}
 
 
 def cpu_baseline(n, seconds_budget, steps_cap):
@@ -197,6 +213,8 @@ def run_gpu(args):
     def run(k):
         return tg.run_steps(W, dx, GAMMA, k, tile=tile)
 
+    clocks = ClockSampler(local)
+    clocks.start()
     # warm-up (W >= 3 enforced)
     for _ in range(max(3, Wu)):
         out = run(2)
@@ -208,16 +226,16 @@ def run_gpu(args):
         torch.cuda.synchronize()
 
     # ---- kernel throughput: K steps, inputs resident, state (2.7 GB) >> L2 ----
-    clocks = ClockSampler(local)
-    clocks.start()
     stream = torch.cuda.current_stream(dev)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     barrier()
+    clocks.mark_start()
     e0.record(stream)
     out, ctl = tg.run_steps(W, dx, GAMMA, K, tile=tile, return_ctl=True)
     e1.record(stream)
     barrier()
+    clocks.mark_stop()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     summ = tg.time_integration.ctl_summary(ctl)

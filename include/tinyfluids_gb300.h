@@ -119,6 +119,55 @@ int tf_evolve_along_axis(const float *W_in, float *W_out, int nx, int ny, int nz
                          float dt_host, const float *dt_dev, float gamma, int axis,
                          unsigned flags, void *stream);
 
+/* ---- batches: many independent instances, each with its own dt ---- */
+
+/* One instance of a batch (host struct; all pointers are device memory).  The
+ * loop per instance is time_integration.py:63-92 with the CFL dt of
+ * fluid.py:427-504 (or fixed_dt > 0), bounded by t_final and/or max_steps. */
+typedef struct tf_instance {
+  const float *W_in; /* initial primitive state [5][nx][ny][nz] */
+  float *W_out;      /* final state */
+  float *work;       /* scratch state, same size */
+  tf_ctl *ctl;       /* this instance's control block (t, dt, iter, status) */
+  int nx, ny, nz;
+  unsigned flags;    /* TF_FLAG_OPEN_BOUNDARIES */
+  float dx, gamma, cfl;
+  float t_final;     /* +inf when only max_steps bounds the loop */
+  float fixed_dt;    /* > 0: fixed dt instead of the CFL dt */
+  int max_steps;     /* < 0: unbounded (t_final must be finite) */
+  int lx;            /* x planes per tile, 0 = default */
+  int reserved;
+} tf_instance;
+
+typedef struct tf_batch_config {
+  int rows;          /* warps per CTA of the fused tile: 8 or 16 */
+  int exact;         /* nonzero: reference op order */
+  int persistent;    /* nonzero: one persistent launch for all steps; else one launch per step */
+  int ctas_per_sm;   /* persistent grid = ctas_per_sm * SMs (0 = occupancy limit) */
+  unsigned long long wait_limit; /* bounded spin before TF_ERR_TIMEOUT (0 = default) */
+} tf_batch_config;
+
+/* Device workspace bytes for a batch of `count` instances (256-byte aligned). */
+unsigned long long tf_batch_workspace_bytes(int count);
+
+/* Validates the instances, builds the tile tables and uploads them to the
+ * workspace (synchronises `stream` once).  No reference counterpart: the
+ * reference advances one state per call (time_integration.py:94-128). */
+int tf_batch_prepare(const tf_instance *inst, int count, const tf_batch_config *cfg,
+                     void *workspace, unsigned long long workspace_bytes, void *stream);
+
+/* Enqueues `steps` step slots of a prepared batch, starting at step_base
+ * (0: also initialises every ctl and computes the first dt).  Asynchronous
+ * and capturable in a CUDA graph.  Each instance's result is in its W_out and
+ * its t/iter/status in its ctl. */
+int tf_batch_run(void *workspace, int step_base, int steps, void *stream);
+
+/* Batch-level device error (TF_ERR_TIMEOUT if a bounded wait gave up); syncs. */
+int tf_batch_error(void *workspace, int *error_host, void *stream);
+
+/* Forgets the host-side plan of a workspace. */
+int tf_batch_release(void *workspace);
+
 /* ---- initial states, built on the device (W: 5*n^3 floats, n^3 grid) ---- */
 
 /* scaling_jax.py:23-41 setup_ics(n, k): rho = 0.125, p = 0.1, u = 0; rho = p = 1

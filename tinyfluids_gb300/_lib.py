@@ -28,6 +28,21 @@ class TileConfig(ctypes.Structure):
     _fields_ = [("rows", c_int), ("lx", c_int)]
 
 
+class Instance(ctypes.Structure):
+    """tf_instance: one member of a batch."""
+    _fields_ = [("W_in", vp), ("W_out", vp), ("work", vp), ("ctl", vp),
+                ("nx", c_int), ("ny", c_int), ("nz", c_int), ("flags", c_uint),
+                ("dx", c_float), ("gamma", c_float), ("cfl", c_float), ("t_final", c_float),
+                ("fixed_dt", c_float), ("max_steps", c_int), ("lx", c_int),
+                ("reserved", c_int)]
+
+
+class BatchConfig(ctypes.Structure):
+    """tf_batch_config."""
+    _fields_ = [("rows", c_int), ("exact", c_int), ("persistent", c_int),
+                ("ctas_per_sm", c_int), ("wait_limit", c_ull)]
+
+
 # name -> (restype, argtypes); mirrors include/tinyfluids_gb300.h
 SIGNATURES = {
     "tf_abi_version": (c_int, []),
@@ -43,6 +58,11 @@ SIGNATURES = {
                                     c_float, c_float, c_int, c_float, c_uint, vp, vp, vp]),
     "tf_evolve_along_axis": (c_int, [vp, vp, c_int, c_int, c_int, c_float, c_float, vp,
                                      c_float, c_int, c_uint, vp]),
+    "tf_batch_workspace_bytes": (c_ull, [c_int]),
+    "tf_batch_prepare": (c_int, [vp, c_int, vp, vp, c_ull, vp]),
+    "tf_batch_run": (c_int, [vp, c_int, c_int, vp]),
+    "tf_batch_error": (c_int, [vp, vp, vp]),
+    "tf_batch_release": (c_int, [vp]),
     "tf_ics_injection_cube": (c_int, [vp, c_int, c_int, vp]),
     "tf_ics_overpressure": (c_int, [vp, c_int, c_ull, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]),

@@ -86,12 +86,14 @@ __device__ __forceinline__ bool ctl_finish_cta(tf_ctl* ctl, float cta_max, unsig
   ctl->max_speed = ms;
   ctl->dt = dt_next;
   ctl->t = t;
-  ctl->iter = iter;
   ctl->status = status;
+  ctl->active = active;
   ctl->ws_bits = 0u;
   ctl->done = 0u;
   __threadfence();
-  ctl->active = active;
+  // iter is written last: a CTA that waits for this step (the persistent
+  // batch kernel) polls iter and then reads the other fields after a fence
+  *(volatile int*)&ctl->iter = iter;
   return true;
 }
 

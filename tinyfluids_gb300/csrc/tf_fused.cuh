@@ -78,7 +78,10 @@ __device__ __forceinline__ void shfl_up_cell(const Cell<T>& in, Cell<T>& out) {
 
 // One CTA-tile of the fused step.  Returns this thread's running maximum of
 // the stored cells' wave speeds (0 for threads that store nothing).
-template <class P, int NW>
+// COHERENT selects L2-only loads (ld.global.cg) for kernels that read data
+// other CTAs wrote earlier in the same launch (the persistent batch kernel);
+// otherwise loads use the read-only path.
+template <class P, int NW, bool COHERENT = false>
 __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float* __restrict__ dst,
                                             const FusedGeom& G, int tz, int ty, int tx,
                                             const StepConsts<float>& K, FusedSmem<NW>& sm) {
@@ -100,7 +103,7 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
   auto load = [&](int x, float v[5]) {
     const float* p = src + (size_t)src_index(x, G.nx, open) * plane + col_src;
 #pragma unroll
-    for (int i = 0; i < 5; ++i) v[i] = __ldg(p + i * vstride);
+    for (int i = 0; i < 5; ++i) v[i] = COHERENT ? __ldcg(p + i * vstride) : __ldg(p + i * vstride);
   };
 
   float wmax = 0.f;
@@ -167,12 +170,12 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
       for (int i = 0; i < 5; ++i) fzh[i] = __shfl_down_sync(0xffffffffu, fzl[i], 1);
       float s3[5], wo[5];
       P::update(cz, fzl, fzh, s3, K);
-      P::to_prim(s3, wo, K);
+      const float sp = P::finish(s3, wo, K);
       if (stores) {
         float* q = dst + (size_t)x * plane + col_dst;
 #pragma unroll
         for (int i = 0; i < 5; ++i) q[i * vstride] = wo[i];
-        wmax = speed_max(wmax, exact_cell_speed(wo, K.g));
+        wmax = speed_max(wmax, sp);
       }
     }
 #pragma unroll

@@ -202,6 +202,13 @@ struct ExactPolicy {
       U[i] = O::add(C.U[i], O::mul(O::mul(k.inv_dx, O::sub(flo[i], fhi[i])), k.dt));
     exact_prim_from_cons(U, s_out, k);
   }
+
+  // Primitive output (the state itself) and its CFL speed, fluid.py:427-500.
+  static __device__ __forceinline__ T finish(const T s[5], T w[5], const StepConsts<T>& k) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) w[i] = s[i];
+    return exact_cell_speed(w, k.g);
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -212,8 +219,19 @@ struct FastPolicy {
   using real = float;
   static constexpr bool kExact = false;
 
-  static __device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
-  static __device__ __forceinline__ float sqrt_(float x) { return __fsqrt_rn(x); }
+  // Single-instruction (MUFU) reciprocal and square root from the PTX ISA:
+  // rcp.approx / sqrt.approx, max error about 1 ulp; operands here are normal
+  // positive floats (densities, pressures, wave-speed sums).
+  static __device__ __forceinline__ float rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+  static __device__ __forceinline__ float sqrt_(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
 
   static __device__ __forceinline__ void to_state(const float w[5], float U[5],
                                                   const StepConsts<float>& k) {
@@ -272,6 +290,22 @@ struct FastPolicy {
                                                 const StepConsts<float>& k) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) s_out[i] = fmaf(k.k, flo[i] - fhi[i], C.U[i]);
+  }
+
+  // Primitive output of a conserved state and its CFL speed max_d |v_d| + c.
+  static __device__ __forceinline__ float finish(const float U[5], float w[5],
+                                                 const StepConsts<float>& k) {
+    float ir = rcp(U[0]);
+    float vx = U[1] * ir, vy = U[2] * ir, vz = U[3] * ir;
+    float ke = 0.5f * fmaf(U[1], vx, fmaf(U[2], vy, U[3] * vz));
+    float p = k.gm1 * (U[4] - ke);
+    w[0] = U[0];
+    w[1] = vx;
+    w[2] = vy;
+    w[3] = vz;
+    w[4] = p;
+    float c = sqrt_(k.g * p * ir);
+    return speed_max(speed_max(fabsf(vx), fabsf(vy)), fabsf(vz)) + c;
   }
 };
 
