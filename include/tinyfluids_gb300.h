@@ -42,6 +42,8 @@ typedef enum tf_status {
 /* flags */
 #define TF_FLAG_OPEN_BOUNDARIES 1u /* fluid.py:571-572 handle_boundaries=True */
 #define TF_FLAG_EXACT 2u           /* reference op order, bit-identical to the oracle */
+#define TF_FLAG_IN_CONSERVED 4u    /* tf_evolve_along_axis, fast policy: input is conserved */
+#define TF_FLAG_OUT_CONSERVED 8u   /* tf_evolve_along_axis, fast policy: output is conserved */
 
 /*
  * Device-resident control block of a run (64 bytes, caller-allocated device
@@ -67,7 +69,7 @@ typedef struct tf_ctl {
 
 /* Tile shape of the fused step kernel; NULL = built-in heuristic. */
 typedef struct tf_tile_config {
-  int rows;  /* warps per CTA incl. the 2 halo rows: 8 or 16 */
+  int rows;  /* grid rows per tile incl. the 1-cell ring: 8, 16, 32 or 34 (rows/2 warps) */
   int lx;    /* x planes per CTA (>= 1) */
 } tf_tile_config;
 
@@ -110,11 +112,13 @@ int tf_time_integration(const float *W_in, float *W_out, float *work, tf_ctl *ct
                         int max_steps, float fixed_dt, unsigned flags,
                         const tf_tile_config *tile, int *iters_host, void *stream);
 
-/* Per-sweep form of fluid.py:508-557 (_evolve_state_along_axis), axis 0..2,
- * on primitive states: reads W_in, writes W_out.  open_boundaries applies
- * the fluid.py:571-572 remap to the input (use it for the x sweep only).
- * Exact (reference op order) unless flags lacks TF_FLAG_EXACT, in which case
- * the fast arithmetic is used.  A step equals the x, y, z sweeps in order. */
+/* Per-sweep form of fluid.py:508-557 (_evolve_state_along_axis), axis 0..2:
+ * reads W_in, writes W_out.  TF_FLAG_OPEN_BOUNDARIES applies the
+ * fluid.py:571-572 remap to the input (use it for the x sweep only).
+ * TF_FLAG_EXACT: reference op order on primitive states.  Otherwise the fast
+ * arithmetic, with TF_FLAG_IN_CONSERVED / TF_FLAG_OUT_CONSERVED selecting a
+ * conserved input/output; x (prim->cons), y (cons->cons), z (cons->prim)
+ * then reproduce the fused fast step bit for bit. */
 int tf_evolve_along_axis(const float *W_in, float *W_out, int nx, int ny, int nz, float dx,
                          float dt_host, const float *dt_dev, float gamma, int axis,
                          unsigned flags, void *stream);
@@ -140,7 +144,7 @@ typedef struct tf_instance {
 } tf_instance;
 
 typedef struct tf_batch_config {
-  int rows;          /* warps per CTA of the fused tile: 8 or 16 */
+  int rows;          /* grid rows per tile: 8, 16, 32 or 34 (see tf_tile_config) */
   int exact;         /* nonzero: reference op order */
   int persistent;    /* nonzero: one persistent launch for all steps; else one launch per step */
   int ctas_per_sm;   /* persistent grid = ctas_per_sm * SMs (0 = occupancy limit) */

@@ -58,7 +58,7 @@ def test_exact_fused_step_bit_identical(tg, shape, hb):
     dx = 0.05
     dt = F._cfl_time_step(W, dx, GAMMA)
     ref = F._evolve_state(W, dx, dt, GAMMA, hb)
-    for tile in (None, (8, 3), (16, 1)):
+    for tile in (None, (8, 3), (16, 1), (32, 2), (34, 5)):
         out = host(tg._evolve_state(dev(W), dx, float(dt), GAMMA, hb, exact=True, tile=tile))
         assert np.array_equal(out, ref), (shape, hb, tile, np.abs(out - ref).max())
 
@@ -138,9 +138,25 @@ def test_fast_step_close_to_reference(tg, shape, hb):
 def test_fast_step_independent_of_tile_shape(tg):
     W = dev(random_state((70, 45, 77), 8))
     outs = [host(tg._evolve_state(W, 0.05, 1e-3, GAMMA, tile=t))
-            for t in (None, (16, 64), (16, 5), (8, 1), (8, 70))]
+            for t in (None, (16, 64), (16, 5), (8, 1), (8, 70), (32, 7), (34, 70), (32, 1))]
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
+
+
+@pytest.mark.parametrize("shape", [(5, 7, 33), (40, 31, 64), (17, 66, 3)])
+@pytest.mark.parametrize("hb", [False, True])
+def test_fast_fused_step_equals_fast_sweeps(tg, shape, hb):
+    """The fused kernel (packed pairs, conserved state between sweeps) and three
+    per-axis fast sweeps run the same op sequence: equal bit for bit."""
+    W = dev(random_state(shape, 31))
+    dt = 2e-3
+    fused = tg._evolve_state(W, 0.05, dt, GAMMA, hb)
+    a = tg._evolve_state_along_axis(W, 0.05, dt, GAMMA, 1, open_boundaries=hb,
+                                    conserved_out=True)
+    b = tg._evolve_state_along_axis(a, 0.05, dt, GAMMA, 2, conserved_in=True,
+                                    conserved_out=True)
+    c = tg._evolve_state_along_axis(b, 0.05, dt, GAMMA, 3, conserved_in=True)
+    assert torch.equal(fused, c)
 
 
 @pytest.mark.parametrize("axis,shift", [(1, 3), (2, -5), (3, 31)])

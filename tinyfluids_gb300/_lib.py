@@ -72,6 +72,8 @@ SIGNATURES = {
 TF_OK = 0
 TF_FLAG_OPEN_BOUNDARIES = 1
 TF_FLAG_EXACT = 2
+TF_FLAG_IN_CONSERVED = 4
+TF_FLAG_OUT_CONSERVED = 8
 
 
 class TinyfluidsError(RuntimeError):

@@ -49,7 +49,7 @@ struct BatchHeader {
 
 struct BatchPlan {  // host mirror of a prepared workspace
   int count = 0;
-  int rows = 16;
+  int rows = 32;
   int exact = 0;
   int persistent = 1;
   int ctas_per_sm = 0;
@@ -170,11 +170,11 @@ __device__ __forceinline__ void tile_coords(const FusedGeom& g, int t, int& tz, 
 }
 
 // One step of every active instance: one CTA per (instance, tile).
-template <class P, int NW>
-__global__ void __launch_bounds__(NW * 32, 1) batch_step_kernel(const BatchInst* __restrict__ inst,
+template <class P, int NWP>
+__global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) batch_step_kernel(const BatchInst* __restrict__ inst,
                                                                 const int* __restrict__ tile_prefix,
                                                                 int count) {
-  __shared__ FusedSmem<NW> sm;
+  __shared__ FusedSmem<NWP> sm;
   int r = blockIdx.x;
   int i = find_instance(tile_prefix, count, r);
   const BatchInst& I = inst[i];
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(NW * 32, 1) batch_step_kernel(const BatchInst*
   setup_step(I, iter, dt, src, dst, K);
   int tz, ty, tx;
   tile_coords(I.geo, r - __ldg(tile_prefix + i), tz, ty, tx);
-  float m = fused_tile<P, NW, false>(src, dst, I.geo, tz, ty, tx, K, sm);
+  float m = fused_tile<P, NWP, false>(src, dst, I.geo, tz, ty, tx, K, sm);
   float bm = block_max(m, sm.red);
   if (threadIdx.x == 0) ctl_finish_cta(I.ctl, bm, (unsigned)I.ntiles, dt, true);
 }
@@ -199,12 +199,12 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // All steps of all instances in one launch (see the file comment).
-template <class P, int NW>
-__global__ void __launch_bounds__(NW * 32, 1)
+template <class P, int NWP>
+__global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP))
     batch_persistent_kernel(BatchHeader* hdr, const BatchInst* __restrict__ inst,
                             const int* __restrict__ tile_prefix, int count, int tiles_per_step,
                             int step_base, int steps, unsigned long long wait_limit) {
-  __shared__ FusedSmem<NW> sm;
+  __shared__ FusedSmem<NWP> sm;
   __shared__ unsigned long long s_item;
   __shared__ int s_go, s_iter;
   __shared__ float s_dt;
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
     setup_step(I, s_iter, dt, src, dst, K);
     int tz, ty, tx;
     tile_coords(I.geo, r - __ldg(tile_prefix + i), tz, ty, tx);
-    float m = fused_tile<P, NW, true>(src, dst, I.geo, tz, ty, tx, K, sm);
+    float m = fused_tile<P, NWP, true>(src, dst, I.geo, tz, ty, tx, K, sm);
     __threadfence();  // this thread's stores before the CTA's completion count
     float bm = block_max(m, sm.red);
     if (threadIdx.x == 0) ctl_finish_cta(I.ctl, bm, (unsigned)I.ntiles, dt, true);
@@ -263,14 +263,14 @@ __global__ void __launch_bounds__(NW * 32, 1)
   }
 }
 
-template <class P, int NW>
+template <class P, int NWP>
 static int occupancy_persistent(int* per_sm) {
   return cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                        per_sm, batch_persistent_kernel<P, NW>, NW * 32, 0),
+                        per_sm, batch_persistent_kernel<P, NWP>, NWP * 32, 0),
                     "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
 }
 
-template <class P, int NW>
+template <class P, int NWP>
 static int launch_batch(const BatchPlan& p, void* ws, int step_base, int steps, cudaStream_t s) {
   Layout L = layout(p.count);
   char* base = (char*)ws;
@@ -280,7 +280,7 @@ static int launch_batch(const BatchPlan& p, void* ws, int step_base, int steps, 
   if (p.persistent) {
     int per_sm = p.ctas_per_sm;
     if (per_sm <= 0) {
-      TF_TRY((occupancy_persistent<P, NW>(&per_sm)));
+      TF_TRY((occupancy_persistent<P, NWP>(&per_sm)));
       if (per_sm < 1) per_sm = 1;
     }
     long long grid = (long long)per_sm * sm_count();
@@ -288,12 +288,12 @@ static int launch_batch(const BatchPlan& p, void* ws, int step_base, int steps, 
     if (grid > total) grid = total;
     if (grid < 1) return TF_OK;
     unsigned long long lim = p.wait_limit ? p.wait_limit : (1ull << 24);
-    batch_persistent_kernel<P, NW><<<(int)grid, NW * 32, 0, s>>>(
+    batch_persistent_kernel<P, NWP><<<(int)grid, NWP * 32, 0, s>>>(
         hdr, inst, tp, p.count, p.tiles_per_step, step_base, steps, lim);
     return launch_check("batch_persistent_kernel");
   }
   for (int k = 0; k < steps; ++k) {
-    batch_step_kernel<P, NW><<<p.tiles_per_step, NW * 32, 0, s>>>(inst, tp, p.count);
+    batch_step_kernel<P, NWP><<<p.tiles_per_step, NWP * 32, 0, s>>>(inst, tp, p.count);
     TF_TRY(launch_check("batch_step_kernel"));
   }
   return TF_OK;
@@ -321,8 +321,8 @@ int tf_batch_prepare(const tf_instance* inst, int count, const tf_batch_config* 
   BatchPlan plan;
   plan.count = count;
   if (cfg) {
-    if (cfg->rows != 8 && cfg->rows != 16)
-      return set_error(TF_ERR_ARG, "batch rows must be 8 or 16 (got %d)", cfg->rows);
+    if (!valid_tile_rows(cfg->rows))
+      return set_error(TF_ERR_ARG, "batch rows must be 8, 16, 32 or 34 (got %d)", cfg->rows);
     plan.rows = cfg->rows;
     plan.exact = cfg->exact ? 1 : 0;
     plan.persistent = cfg->persistent ? 1 : 0;
@@ -430,13 +430,10 @@ int tf_batch_run(void* workspace, int step_base, int steps, void* stream) {
     // continuation: only the queue restarts
     TF_TRY(cuda_check(cudaMemsetAsync(hdr, 0, sizeof(unsigned long long), s), "cudaMemsetAsync"));
   }
-  if (p.exact) {
-    if (p.rows == 16) TF_TRY((launch_batch<ExactPolicy<float>, 16>(p, workspace, step_base, steps, s)));
-    else TF_TRY((launch_batch<ExactPolicy<float>, 8>(p, workspace, step_base, steps, s)));
-  } else {
-    if (p.rows == 16) TF_TRY((launch_batch<FastPolicy, 16>(p, workspace, step_base, steps, s)));
-    else TF_TRY((launch_batch<FastPolicy, 8>(p, workspace, step_base, steps, s)));
-  }
+  TF_DISPATCH_ROWS(p.rows, NWP, {
+    if (p.exact) TF_TRY((launch_batch<ExactPair, NWP>(p, workspace, step_base, steps, s)));
+    else TF_TRY((launch_batch<FastPair, NWP>(p, workspace, step_base, steps, s)));
+  });
   batch_final_kernel<<<grid_chunks, 256, 0, s>>>(inst, cp, p.count, p.chunks_total);
   return launch_check("batch_final_kernel");
 }

@@ -23,6 +23,34 @@ int sm_count();  // multiprocessors of the current device (cached per device)
 
 }  // namespace tf
 
+// Tile heights (grid rows incl. the one-cell ring) the fused kernel is
+// instantiated for; the kernel uses rows/2 warps.
+inline bool valid_tile_rows(int rows) { return rows == 8 || rows == 16 || rows == 32 || rows == 34; }
+
+// CTAs per SM the fused kernels are register-bounded for: 16 warps per SM
+// for every tile height.
+__host__ __device__ constexpr int min_ctas_per_sm(int nwp) { return nwp >= 16 ? 1 : 16 / nwp; }
+
+#define TF_DISPATCH_ROWS(rows, NWP, ...)          \
+  switch (rows) {                                 \
+    case 8: {                                     \
+      constexpr int NWP = 4;                      \
+      __VA_ARGS__;                                \
+    } break;                                      \
+    case 16: {                                    \
+      constexpr int NWP = 8;                      \
+      __VA_ARGS__;                                \
+    } break;                                      \
+    case 32: {                                    \
+      constexpr int NWP = 16;                     \
+      __VA_ARGS__;                                \
+    } break;                                      \
+    default: {                                    \
+      constexpr int NWP = 17;                     \
+      __VA_ARGS__;                                \
+    } break;                                      \
+  }
+
 #define TF_TRY(expr)              \
   do {                            \
     int _st = (expr);             \

@@ -160,9 +160,9 @@ struct FusedArgs {
   int loop;        // 1: predicated loop step (parity buffers, dt from ctl)
 };
 
-template <class P, int NW>
-__global__ void __launch_bounds__(NW * 32, 1) fused_step_kernel(FusedArgs a) {
-  __shared__ FusedSmem<NW> sm;
+template <class P, int NWP>
+__global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_kernel(FusedArgs a) {
+  __shared__ FusedSmem<NWP> sm;
   const float* src;
   float* dst;
   float dt;
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(NW * 32, 1) fused_step_kernel(FusedArgs a) {
   K.inv_dx = a.inv_dx;
   K.dt = dt;
   K.k = dt * a.inv_dx;
-  float m = fused_tile<P, NW>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z, K, sm);
+  float m = fused_tile<P, NWP>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z, K, sm);
   if (a.ctl) {
     float bm = block_max(m, sm.red);
     if (threadIdx.x == 0)
@@ -233,11 +233,11 @@ static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int
 }
 
 static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx) {
-  *rows = 16;
+  *rows = 32;
   *lx = 0;
   if (tile) {
-    if (tile->rows != 8 && tile->rows != 16)
-      return set_error(TF_ERR_ARG, "tile rows must be 8 or 16 (got %d)", tile->rows);
+    if (!valid_tile_rows(tile->rows))
+      return set_error(TF_ERR_ARG, "tile rows must be 8, 16, 32 or 34 (got %d)", tile->rows);
     *rows = tile->rows;
     *lx = tile->lx;
     if (*lx < 0) return set_error(TF_ERR_ARG, "tile lx must be >= 0");
@@ -249,13 +249,10 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
   if (a.geo.tiles_y > 65535 || a.geo.tiles_x > 65535)
     return set_error(TF_ERR_ARG, "grid too large for the tile grid");
   dim3 grid(a.geo.tiles_z, a.geo.tiles_y, a.geo.tiles_x);
-  if (exact) {
-    if (rows == 16) fused_step_kernel<ExactPolicy<float>, 16><<<grid, 16 * 32, 0, s>>>(a);
-    else fused_step_kernel<ExactPolicy<float>, 8><<<grid, 8 * 32, 0, s>>>(a);
-  } else {
-    if (rows == 16) fused_step_kernel<FastPolicy, 16><<<grid, 16 * 32, 0, s>>>(a);
-    else fused_step_kernel<FastPolicy, 8><<<grid, 8 * 32, 0, s>>>(a);
-  }
+  TF_DISPATCH_ROWS(rows, NWP, {
+    if (exact) fused_step_kernel<ExactPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
+    else fused_step_kernel<FastPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
+  });
   return launch_check("fused_step_kernel");
 }
 
@@ -509,6 +506,10 @@ int tf_evolve_along_axis(const float* W_in, float* W_out, int nx, int ny, int nz
   StepConsts<float> K = make_consts<float>(gamma, dx, dt_host);
   long long n = (long long)nx * ny * nz;
   int open = (flags & TF_FLAG_OPEN_BOUNDARIES) ? 1 : 0;
+  int in_prim = (flags & TF_FLAG_IN_CONSERVED) ? 0 : 1;
+  int out_prim = (flags & TF_FLAG_OUT_CONSERVED) ? 0 : 1;
+  if ((flags & TF_FLAG_EXACT) && !(in_prim && out_prim))
+    return set_error(TF_ERR_ARG, "the exact sweep works on primitive states only");
   cudaStream_t s = (cudaStream_t)stream;
   int grid = elementwise_grid(n);
   if (flags & TF_FLAG_EXACT) {
@@ -516,9 +517,9 @@ int tf_evolve_along_axis(const float* W_in, float* W_out, int nx, int ny, int nz
     if (axis == 1) sweep_kernel<ExactPolicy<float>, 2><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
     if (axis == 2) sweep_kernel<ExactPolicy<float>, 3><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
   } else {
-    if (axis == 0) sweep_kernel<FastPolicy, 1><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
-    if (axis == 1) sweep_kernel<FastPolicy, 2><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
-    if (axis == 2) sweep_kernel<FastPolicy, 3><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
+    if (axis == 0) sweep_kernel<FastPolicy, 1><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
+    if (axis == 1) sweep_kernel<FastPolicy, 2><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
+    if (axis == 2) sweep_kernel<FastPolicy, 3><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
   }
   return launch_check("sweep_kernel");
 }

@@ -174,10 +174,13 @@ def _evolve_state(primitive_state, grid_spacing, dt, gamma, handle_boundaries=Fa
 
 
 def _evolve_state_along_axis(primitive_state, grid_spacing, dt, gamma, axis, *,
-                             exact=None, open_boundaries=False):
+                             exact=None, open_boundaries=False, conserved_in=False,
+                             conserved_out=False):
     """fluid.py:508-557: one periodic HLL sweep along ``axis`` (X_AXIS, Y_AXIS or
     Z_AXIS).  ``open_boundaries`` applies the handle_boundaries remap to the
-    input first (the x sweep of an open-boundary step)."""
+    input first (the x sweep of an open-boundary step).  With the fast
+    arithmetic, ``conserved_in``/``conserved_out`` take/return conserved
+    states, so that x (prim->cons), y, z (cons->prim) equal the fused step."""
     W = check_state(primitive_state)
     if axis not in (X_AXIS, Y_AXIS, Z_AXIS):
         raise ValueError("axis must be X_AXIS, Y_AXIS or Z_AXIS")
@@ -187,7 +190,9 @@ def _evolve_state_along_axis(primitive_state, grid_spacing, dt, gamma, axis, *,
         dt_host, dt_dev, keep = _dt_args(dt, W.device)
         _lib.call("tf_evolve_along_axis", W.data_ptr(), out.data_ptr(), nx, ny, nz,
                   float(grid_spacing), dt_host, dt_dev, _scalar(gamma, "gamma"), axis - 1,
-                  _flags(open_boundaries, exact), _stream(W))
+                  _flags(open_boundaries, exact)
+                  | (_lib.TF_FLAG_IN_CONSERVED if conserved_in else 0)
+                  | (_lib.TF_FLAG_OUT_CONSERVED if conserved_out else 0), _stream(W))
         del keep
     return out
 
