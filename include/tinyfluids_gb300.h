@@ -131,7 +131,7 @@ int tf_evolve_along_axis(const float *W_in, float *W_out, int nx, int ny, int nz
 typedef struct tf_instance {
   const float *W_in; /* initial primitive state [5][nx][ny][nz] */
   float *W_out;      /* final state */
-  float *work;       /* scratch state, same size */
+  float *work;       /* scratch state, same size; may equal W_in (W_in is then overwritten) */
   tf_ctl *ctl;       /* this instance's control block (t, dt, iter, status) */
   int nx, ny, nz;
   unsigned flags;    /* TF_FLAG_OPEN_BOUNDARIES */

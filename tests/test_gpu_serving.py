@@ -1,0 +1,65 @@
+"""Continuous-batching server: results equal each request run alone (bit for
+bit), admission respects the HBM budget, and arrivals during a run join it."""
+import pytest
+import torch
+
+from tinyfluids_gb300 import serving
+from tinyfluids_gb300.serving import Request, Server
+
+pytestmark = pytest.mark.gpu
+GAMMA = 5.0 / 3.0
+
+
+def alone(tg, r):
+    W, dx = serving.build_initial_state(r, torch.device("cuda"))
+    return tg.run_steps(W, dx, GAMMA, r.steps)
+
+
+def test_served_results_equal_alone(tg):
+    reqs = [Request(0, 24, 13, "overpressure", 1, 0.0), Request(1, 40, 30, "shear", 2, 0.0),
+            Request(2, 33, 7, "shear", 3, 0.0), Request(3, 17, 22, "overpressure", 4, 0.0),
+            Request(4, 28, 1, "overpressure", 5, 0.0)]
+    srv = Server(hbm_budget=8e9, tick_steps=5, keep_states=True)
+    done = srv.serve(reqs)
+    assert len(done) == len(reqs)
+    for r in done:
+        assert torch.equal(r.result["state"], alone(tg, r)), r.rid
+    assert srv.used == 0 and not srv.active
+
+
+def test_budget_limits_concurrency_and_late_arrivals_join(tg):
+    reqs = [Request(i, 32, 12 + 3 * i, "overpressure" if i % 2 else "shear", i, 0.002 * i)
+            for i in range(6)]
+    budget = 2 * serving.request_bytes(32) + 100
+    srv = Server(hbm_budget=budget, tick_steps=4, keep_states=True)
+    seen = []
+    orig = srv._tick
+
+    def tick():
+        seen.append(len(srv.active))
+        orig()
+    srv._tick = tick
+    done = srv.serve(reqs)
+    assert max(seen) <= 2 and len(done) == 6
+    for r in done:
+        assert r.finished >= r.arrival
+        assert torch.equal(r.result["state"], alone(tg, r))
+
+
+def test_one_at_a_time_baseline_and_stats(tg):
+    reqs = serving.poisson_requests(6, rate=200.0, seed=3, n_range=(16, 32), steps_range=(3, 9))
+    base = serving.serve_one_at_a_time([Request(r.rid, r.n, r.steps, r.ic, r.seed, r.arrival)
+                                        for r in reqs])
+    st = serving.latency_stats(base)
+    assert st["solves"] == 6 and st["p99_s"] >= st["p50_s"] > 0
+    srv = Server(hbm_budget=1e9, tick_steps=4)
+    done = srv.serve(reqs)
+    by_id = {r.rid: r for r in base}
+    for r in done:  # same physics either way (mass is conserved and equal)
+        assert r.result["mass"] == by_id[r.rid].result["mass"]
+
+
+def test_oversized_request_rejected(tg):
+    srv = Server(hbm_budget=1e6)
+    with pytest.raises(ValueError):
+        srv.submit(Request(0, 64, 10))

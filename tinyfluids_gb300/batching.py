@@ -33,14 +33,17 @@ class InstanceSpec:
     C_CFL: float = 0.4
     handle_boundaries: bool = False
     lx: int = 0                     # x planes per tile (0: default)
+    out: torch.Tensor | None = None   # preallocated result buffer (else allocated)
+    consume_input: bool = False     # use the input as scratch (it is overwritten)
 
 
 class Batch:
     """A prepared batch; ``run()`` advances every instance and returns the
     final states (new tensors, inputs untouched)."""
 
-    def __init__(self, specs, *, rows=16, exact=None, persistent=True, ctas_per_sm=0,
+    def __init__(self, specs, *, rows=32, exact=None, persistent=True, ctas_per_sm=0,
                  wait_limit=0, capture_graph=False, steps=None):
+        self._closed = True
         if not specs:
             raise ValueError("a batch needs at least one instance")
         self.specs = list(specs)
@@ -64,8 +67,13 @@ class Batch:
         self.steps = int(steps)
         with torch.cuda.device(dev):
             self.inputs = [check_state(sp.state) for sp in self.specs]
-            self.outputs = [torch.empty_like(W) for W in self.inputs]
-            self.works = [torch.empty_like(W) for W in self.inputs]
+            self.outputs = [sp.out if sp.out is not None else torch.empty_like(W)
+                            for sp, W in zip(self.specs, self.inputs)]
+            for o, W in zip(self.outputs, self.inputs):
+                if o.shape != W.shape or o.dtype != W.dtype or not o.is_contiguous():
+                    raise ValueError("out must be a contiguous tensor like the state")
+            self.works = [W if sp.consume_input else torch.empty_like(W)
+                          for sp, W in zip(self.specs, self.inputs)]
             self.ctls = [new_ctl(dev) for _ in self.specs]
             n = len(self.specs)
             arr = (_lib.Instance * n)()
@@ -87,6 +95,7 @@ class Batch:
             _lib.call("tf_batch_prepare", ctypes.cast(arr, ctypes.c_void_p), n,
                       ctypes.byref(cfg), self.workspace.data_ptr(), nbytes,
                       self._stream.cuda_stream)
+            self._closed = False
         self.graph = None
         if capture_graph:
             self.capture()
@@ -133,7 +142,11 @@ class Batch:
         return [ctl_summary(c) for c in self.ctls]
 
     def close(self):
-        _lib.load().tf_batch_release(ctypes.c_void_p(self.workspace.data_ptr()))
+        """Forget the C-side plan (once; the workspace stays allocated until the
+        object dies, so its address cannot be reused before this)."""
+        if not self._closed:
+            self._closed = True
+            _lib.load().tf_batch_release(ctypes.c_void_p(self.workspace.data_ptr()))
 
     def __del__(self):
         try:

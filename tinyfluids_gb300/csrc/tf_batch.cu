@@ -112,7 +112,8 @@ __global__ void batch_init_kernel(BatchHeader* hdr, const BatchInst* __restrict_
 // Max wave speed of every instance's initial state; sets each ctl's dt.
 __global__ void __launch_bounds__(256) batch_maxspeed_kernel(const BatchInst* __restrict__ inst,
                                                              const int* __restrict__ chunk_prefix,
-                                                             int count, int chunks_total) {
+                                                             int count, int chunks_total,
+                                                             int fast) {
   __shared__ float red[8];
   for (int c = blockIdx.x; c < chunks_total; c += gridDim.x) {
     int i = find_instance(chunk_prefix, count, c);
@@ -124,7 +125,7 @@ __global__ void __launch_bounds__(256) batch_maxspeed_kernel(const BatchInst* __
       float w[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) w[v] = __ldg(I.src0 + v * I.ncells + j);
-      m = speed_max(m, exact_cell_speed(w, I.gamma));
+      m = speed_max(m, fast ? FastPolicy::cell_speed(w, I.gamma) : exact_cell_speed(w, I.gamma));
     }
     float bm = block_max(m, red);
     if (threadIdx.x == 0) ctl_finish_cta(I.ctl, bm, (unsigned)I.nchunks, 0.f, false);
@@ -338,8 +339,8 @@ int tf_batch_prepare(const tf_instance* inst, int count, const tf_batch_config* 
     const tf_instance& q = inst[i];
     if (!q.W_in || !q.W_out || !q.work || !q.ctl)
       return set_error(TF_ERR_ARG, "instance %d: null pointer", i);
-    if (q.W_in == q.W_out || q.W_in == q.work || q.W_out == q.work)
-      return set_error(TF_ERR_ARG, "instance %d: W_in, W_out, work must be distinct", i);
+    if (q.W_in == q.W_out || q.W_out == q.work)
+      return set_error(TF_ERR_ARG, "instance %d: W_out must differ from W_in and work", i);
     if (q.nx < 1 || q.ny < 1 || q.nz < 1) return set_error(TF_ERR_ARG, "instance %d: bad dims", i);
     if ((q.flags & TF_FLAG_OPEN_BOUNDARIES) && (q.nx < 2 || q.ny < 2 || q.nz < 2))
       return set_error(TF_ERR_ARG, "instance %d: open boundaries need >= 2 cells per axis", i);
@@ -362,8 +363,9 @@ int tf_batch_prepare(const tf_instance* inst, int count, const tf_batch_config* 
     g.tiles_x = (q.nx + lx - 1) / lx;
     b.geo = g;
     b.src0 = q.W_in;
-    // with a known step count the last step writes W_out directly
-    bool even = q.max_steps >= 0 && (q.max_steps & 1) == 0;
+    // with a known step count the last step writes W_out directly; when work
+    // aliases W_in (the input may be overwritten), step 1 must write W_out
+    bool even = q.work != q.W_in && q.max_steps >= 0 && (q.max_steps & 1) == 0;
     b.buf[0] = even ? q.W_out : q.work;
     b.buf[1] = even ? q.work : q.W_out;
     b.out = q.W_out;
@@ -424,7 +426,8 @@ int tf_batch_run(void* workspace, int step_base, int steps, void* stream) {
   if (step_base == 0) {
     batch_init_kernel<<<(p.count + 255) / 256, 256, 0, s>>>(hdr, inst, p.count);
     TF_TRY(launch_check("batch_init_kernel"));
-    batch_maxspeed_kernel<<<grid_chunks, 256, 0, s>>>(inst, cp, p.count, p.chunks_total);
+    batch_maxspeed_kernel<<<grid_chunks, 256, 0, s>>>(inst, cp, p.count, p.chunks_total,
+                                                      p.exact ? 0 : 1);
     TF_TRY(launch_check("batch_maxspeed_kernel"));
   } else {
     // continuation: only the queue restarts

@@ -292,6 +292,15 @@ struct FastPolicy {
     for (int i = 0; i < 5; ++i) s_out[i] = fmaf(k.k, flo[i] - fhi[i], C.U[i]);
   }
 
+  // CFL speed max_d |v_d| + c of a stored primitive cell, computed exactly
+  // as finish() computes it for the cell it stores (same ir and p), so a run
+  // restarted from a stored state reproduces the uninterrupted dt sequence.
+  static __device__ __forceinline__ float cell_speed(const float w[5], float g) {
+    float ir = rcp(w[0]);
+    float c = sqrt_(g * w[4] * ir);
+    return speed_max(speed_max(fabsf(w[1]), fabsf(w[2])), fabsf(w[3])) + c;
+  }
+
   // Primitive output of a conserved state and its CFL speed max_d |v_d| + c.
   static __device__ __forceinline__ float finish(const float U[5], float w[5],
                                                  const StepConsts<float>& k) {

@@ -107,9 +107,11 @@ __global__ void ctl_init_kernel(tf_ctl* ctl, float t_final, float cfl_dx, int ma
 }
 
 // Max wave speed of a primitive state (fluid.py:427-500 in per-cell form);
-// the last CTA sets ctl->dt and the loop condition.
+// the last CTA sets ctl->dt and the loop condition.  `fast` selects the fast
+// policy's speed formula (the one its fused epilogue uses) for loops run with
+// the fast arithmetic; otherwise the reference's.
 __global__ void __launch_bounds__(256) maxspeed_kernel(const float* __restrict__ W, long long n,
-                                                       float g, tf_ctl* ctl) {
+                                                       float g, tf_ctl* ctl, int fast) {
   __shared__ float red[8];
   float m = 0.f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(256) maxspeed_kernel(const float* __restrict__
     float w[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) w[v] = __ldg(W + v * n + i);
-    m = speed_max(m, exact_cell_speed(w, g));
+    m = speed_max(m, fast ? FastPolicy::cell_speed(w, g) : exact_cell_speed(w, g));
   }
   float bm = block_max(m, red);
   if (threadIdx.x == 0) ctl_finish_cta(ctl, bm, gridDim.x, 0.f, false);
@@ -380,7 +382,7 @@ int tf_cfl_time_step(const float* W, int nx, int ny, int nz, float dx, float gam
   long long n = (long long)nx * ny * nz;
   float cfl_dx = cfl * dx;  // fluid.py:502, rounded to float like the traced product
   ctl_init_kernel<<<1, 1, 0, s>>>(ctl, 0.f, cfl_dx, 0);
-  maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W, n, gamma, ctl);
+  maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W, n, gamma, ctl, 0);
   return launch_check("maxspeed_kernel");
 }
 
@@ -424,7 +426,7 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
   const bool exact = (flags & TF_FLAG_EXACT) != 0;
 
   ctl_init_kernel<<<1, 1, 0, s>>>(ctl, t_final, cfl * dx, max_steps);
-  maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W_in, n, gamma, ctl);
+  maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W_in, n, gamma, ctl, exact ? 0 : 1);
   TF_TRY(launch_check("maxspeed_kernel"));
 
   FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
