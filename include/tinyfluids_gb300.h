@@ -123,6 +123,24 @@ int tf_evolve_along_axis(const float *W_in, float *W_out, int nx, int ny, int nz
                          float dt_host, const float *dt_dev, float gamma, int axis,
                          unsigned flags, void *stream);
 
+/* Largest grid (nx*ny*nz cells) tf_time_integration_noalloc accepts. */
+#define TF_NOALLOC_MAX_CELLS (1 << 18)
+
+/* The run loop of tf_time_integration for callers that cannot allocate device
+ * memory (a host runtime that owns the device heap, allocator-free callbacks,
+ * memory reserved up front): the work state and control block come from a
+ * fixed scratch array compiled into the library (about 5 MiB per GPU that
+ * loads it, held until exit), so the caller passes only W_in and W_out, and
+ * nothing is allocated.  Grids above TF_NOALLOC_MAX_CELLS cells are rejected
+ * with TF_ERR_ARG.  The first call on a device looks up the scratch's device
+ * address; make that first call before any stream capture.  All calls share
+ * the one scratch array: calls that may overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller.  No counterpart
+ * in the reference (it has no allocation control). */
+int tf_time_integration_noalloc(const float *W_in, float *W_out, int nx, int ny, int nz,
+                                float dx, float t_final, float gamma, float cfl, int max_steps,
+                                float fixed_dt, unsigned flags, int *iters_host, void *stream);
+
 /* ---- batches: many independent instances, each with its own dt ---- */
 
 /* One instance of a batch (host struct; all pointers are device memory).  The

@@ -527,3 +527,126 @@ int tf_evolve_along_axis(const float* W_in, float* W_out, int nx, int ny, int nz
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free run (tf_time_integration_noalloc)
+// ===========================================================================
+// Some callers cannot allocate device memory at the point where they step a
+// simulation: code running inside a host runtime that owns the device heap and
+// forbids outside cudaMalloc/cudaFree, callbacks that must not block on the
+// allocator, or programs that reserved all memory up front.  For them the run
+// loop's scratch -- one control block and one work state -- lives in a
+// file-scope device array instead of caller or library allocations.  Every GPU
+// that loads this library holds the array (about 5 MiB) until the process
+// exits.
+namespace tf {
+constexpr size_t kNoallocCtlBytes = 256;
+constexpr size_t kNoallocBytes =
+    kNoallocCtlBytes + 5 * sizeof(float) * (size_t)TF_NOALLOC_MAX_CELLS;
+static __device__ __align__(256) unsigned char tf_noalloc_scratch[kNoallocBytes];
+
+// Device address of the scratch on the current device.  In host code the
+// array's name is only a host-side handle, so it is looked up once per device
+// (with that device current) and cached.
+constexpr int kNoallocMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[kNoallocMaxDevices] = {};
+
+static int noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  TF_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
+  if (dev < 0 || dev >= kNoallocMaxDevices)
+    return set_error(TF_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    TF_TRY(cuda_check(cudaGetSymbolAddress(&p, tf_noalloc_scratch),
+                      "cudaGetSymbolAddress(tf_noalloc_scratch)"));
+    g_noalloc_addr[dev] = p;
+  }
+  *out = (unsigned char*)g_noalloc_addr[dev];
+  return TF_OK;
+}
+}  // namespace tf
+
+extern "C" int tf_time_integration_noalloc(const float* W_in, float* W_out, int nx, int ny,
+                                           int nz, float dx, float t_final, float gamma,
+                                           float cfl, int max_steps, float fixed_dt,
+                                           unsigned flags, int* iters_host, void* stream) {
+  if (!W_in || !W_out) return set_error(TF_ERR_ARG, "null state pointer");
+  if (W_in == W_out) return set_error(TF_ERR_ARG, "W_out must not alias W_in");
+  TF_TRY(check_dims(nx, ny, nz, flags));
+  const long long n = (long long)nx * ny * nz;
+  if (n > (long long)TF_NOALLOC_MAX_CELLS)
+    return set_error(TF_ERR_ARG,
+                     "grid of %lld cells exceeds the allocation-free scratch of %d cells "
+                     "(use tf_time_integration with a caller-provided work buffer)",
+                     n, (int)TF_NOALLOC_MAX_CELLS);
+  TF_TRY(check_scalars(dx, gamma));
+  if (!(cfl > 0.f) || !isfinite(cfl)) return set_error(TF_ERR_ARG, "C_CFL must be finite and > 0");
+  if (isnan(t_final)) return set_error(TF_ERR_ARG, "t_final is NaN");
+  if (!(fixed_dt >= 0.f) || !isfinite(fixed_dt)) return set_error(TF_ERR_ARG, "fixed_dt must be >= 0");
+  if (max_steps < 0 && !isfinite(t_final))
+    return set_error(TF_ERR_ARG, "an unbounded loop needs a finite t_final or max_steps >= 0");
+  unsigned char* scratch = nullptr;
+  TF_TRY(noalloc_scratch(&scratch));
+  tf_ctl* ctl = (tf_ctl*)scratch;
+  float* work = (float*)(scratch + kNoallocCtlBytes);
+  if (W_out == work || W_in == work) return set_error(TF_ERR_ARG, "states must not be the scratch");
+
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool exact = (flags & TF_FLAG_EXACT) != 0;
+  int rows = 32, lx = 0;
+  // the control block keeps the previous call's contents: re-initialise all of it
+  ctl_init_kernel<<<1, 1, 0, s>>>(ctl, t_final, cfl * dx, max_steps);
+  maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W_in, n, gamma, ctl, exact ? 0 : 1);
+  TF_TRY(launch_check("maxspeed_kernel"));
+  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
+  float* b0 = work;
+  float* b1 = W_out;
+  if (max_steps >= 0 && (max_steps & 1) == 0) {
+    b0 = W_out;
+    b1 = work;
+  }
+  FusedArgs a = make_fused_args(W_in, b0, b1, geo, dx, gamma);
+  a.loop = 1;
+  a.ctl = ctl;
+  a.fixed_dt = fixed_dt;
+  if (max_steps >= 0) {
+    for (int i = 0; i < max_steps; ++i) TF_TRY(launch_fused(a, rows, exact, s));
+  } else {
+    tf_ctl h;  // host copy of the loop state (pageable, on the stack)
+    int chunk = 8;
+    long long launched = 0;
+    float t_prev = -1.f;
+    for (;;) {
+      for (int i = 0; i < chunk; ++i) TF_TRY(launch_fused(a, rows, exact, s));
+      launched += chunk;
+      TF_TRY(cuda_check(cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, s),
+                        "cudaMemcpyAsync(ctl)"));
+      TF_TRY(cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
+      if (!h.active) break;
+      if (h.t == t_prev)
+        return set_error(TF_ERR_NONFINITE, "time stalled at t=%g", (double)h.t);
+      t_prev = h.t;
+      if (launched > (1LL << 28)) return set_error(TF_ERR_ARG, "loop did not terminate");
+      double rem = h.dt > 0.f ? ((double)t_final - h.t) / h.dt : 8.0;
+      double want = rem * 1.1 + 2.0;
+      chunk = want < 4 ? 4 : (want > 512 ? 512 : (int)want);
+    }
+  }
+  final_select_kernel<<<elementwise_grid(5 * n / 4 + 1), 256, 0, s>>>(ctl, W_in, b0, b1, W_out,
+                                                                       5 * n);
+  TF_TRY(launch_check("final_select_kernel"));
+  if (iters_host) {
+    tf_ctl h;
+    TF_TRY(cuda_check(cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, s),
+                      "cudaMemcpyAsync(ctl)"));
+    TF_TRY(cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
+    *iters_host = h.iter;
+    if (h.status != TF_OK)
+      return set_error(h.status, "device reported %s after %d steps", tf_status_string(h.status),
+                       h.iter);
+  }
+  return TF_OK;
+}
