@@ -49,6 +49,13 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--tile", default=None, help="rows,lx of the fused kernel")
     p.add_argument("--out", default=None, help="also write the JSON line here")
+    p.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "adjoint"],
+                   help="plain: 512^3 step (default); batch: 256 uneven instances in one "
+                        "persistent launch; serve: continuous batching vs one-at-a-time; "
+                        "adjoint: 128^3 fixed-dt gradient")
+    p.add_argument("--instances", type=int, default=256)
+    p.add_argument("--requests", type=int, default=120)
+    p.add_argument("--rates", default="10,50,100,200,500")
     return p.parse_args()
 
 
@@ -194,7 +201,7 @@ def run_gpu(args):
     import torch
 
     import tinyfluids_gb300 as tg
-    from tinyfluids_gb300 import build
+    from tinyfluids_gb300 import build, replicas
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -241,12 +248,8 @@ def run_gpu(args):
     summ = tg.time_integration.ctl_summary(ctl)
     if summ["status"] != 0 or summ["iter"] != K:
         raise RuntimeError(f"run failed: {summ}")
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t)
     cells = n ** 3
-    value = world * cells * K / (ms * 1e-3) / 1e9
+    value, ms = replicas.job_throughput(cells, K, ms, world, dev)
 
     # ---- end to end: public API with pinned host buffers ----
     Wh = W.cpu().pin_memory()
@@ -263,12 +266,7 @@ def run_gpu(args):
         b.record(stream)
         barrier()
         e2e_ms.append(a.elapsed_time(b))
-    e2e = min(e2e_ms)
-    if dist is not None:
-        t = torch.tensor([e2e], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e = float(t)
-    e2e_value = world * cells * K / (e2e * 1e-3) / 1e9
+    e2e_value, e2e = replicas.job_throughput(cells, K, min(e2e_ms), world, dev)
 
     if rank != 0:
         return 0
@@ -319,10 +317,168 @@ def run_gpu(args):
     return 0
 
 
+def _gpu_setup():
+    import torch
+    import tinyfluids_gb300 as tg
+    from tinyfluids_gb300 import build
+    build.build()
+    tg._lib.load()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    return torch, tg, dev
+
+
+def run_batch_workload(args):
+    """Config 3: `instances` overpressure spheres, N uniform in {32,48,64,96,128},
+    radius U[0.05,0.2], pressure ratio U[10,100] (p_out 0.1), +-1% rho noise,
+    100 CFL steps each with its own dt, in one persistent graph-captured launch;
+    against the plain loop of one run_steps call per instance."""
+    import numpy as np
+    torch, tg, dev = _gpu_setup()
+    from tinyfluids_gb300.batching import Batch, InstanceSpec
+    rng = np.random.default_rng(0)
+    K = args.steps if args.steps != 200 else 100
+    specs = []
+    for i in range(args.instances):
+        n = int(rng.choice([32, 48, 64, 96, 128]))
+        ratio = float(rng.uniform(10, 100))
+        W, dx = tg.overpressure(n, seed=i, radius=float(rng.uniform(0.05, 0.2)),
+                               p_in=0.1 * ratio, p_out=0.1, device=dev)
+        specs.append(InstanceSpec(W, dx, GAMMA, num_steps=K))
+    cells = sum(sp.state[0].numel() for sp in specs) * K
+    b = Batch(specs, autotune=True, capture_graph=True)
+    for _ in range(max(3, args.warmup)):
+        b.run()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    outs = b.run()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms_batch = e0.elapsed_time(e1)
+    assert b.error() == 0 and all(s["iter"] == K for s in b.summaries())
+    # plain loop: one run_steps per instance (tuned tile per size)
+    for sp in specs[:8]:
+        tg.run_steps(sp.state, sp.grid_spacing, GAMMA, K, tile="auto")
+    torch.cuda.synchronize()
+    e0.record(st)
+    alone = [tg.run_steps(sp.state, sp.grid_spacing, GAMMA, K, tile="auto") for sp in specs]
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms_plain = e0.elapsed_time(e1)
+    same = all(torch.equal(o, a) for o, a in zip(outs, alone))
+    line = {"metric": "batched solves/s (256 uneven instances, 100 CFL steps each)",
+            "value": args.instances / (ms_batch * 1e-3), "unit": "solves/s",
+            "higher_is_better": True, "n_gpus": 1, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{args.instances} overpressure instances, N in "
+                                   "{32,48,64,96,128}, 100 steps, persistent launch",
+                       "rows": b.rows},
+            "gcell_updates_per_s": cells / (ms_batch * 1e-3) / 1e9, "ms": ms_batch,
+            "plain_loop": {"solves_per_s": args.instances / (ms_plain * 1e-3), "ms": ms_plain,
+                           "gcell_updates_per_s": cells / (ms_plain * 1e-3) / 1e9},
+            "speedup_vs_plain_loop": ms_plain / ms_batch,
+            "results_equal_alone": bool(same)}
+    emit(line, args.out)
+    return 0
+
+
+def run_serve_workload(args):
+    """Config 4: Poisson arrivals over a rate sweep; N uniform in [32,256],
+    steps uniform in [50,500], seeded overpressure or shear states, 120 GB
+    budget; continuous batching against the plain one-solve-at-a-time loop."""
+    torch, tg, dev = _gpu_setup()
+    from tinyfluids_gb300 import serving
+    rates = [float(r) for r in args.rates.split(",")]
+    sweep = []
+    for rate in rates:
+        reqs = serving.poisson_requests(args.requests, rate, seed=int(rate))
+        srv = serving.Server(hbm_budget=120e9, device=dev)
+        st = serving.latency_stats(srv.serve(reqs))
+        base = serving.serve_one_at_a_time(
+            [serving.Request(r.rid, r.n, r.steps, r.ic, r.seed, r.arrival) for r in reqs],
+            device=dev)
+        bt = serving.latency_stats(base)
+        sweep.append({"rate": rate, "served": st, "one_at_a_time": bt, "ticks": srv.ticks,
+                      "solves_per_s_ratio": st["solves_per_s"] / bt["solves_per_s"]})
+    top = sweep[-1]
+    line = {"metric": "served solves/s, p50/p99 latency (continuous batching)",
+            "value": top["served"]["solves_per_s"], "unit": "solves/s", "higher_is_better": True,
+            "n_gpus": 1, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{args.requests} requests per rate, N U[32,256], steps "
+                                   "U[50,500], 120 GB budget", "rates": rates},
+            "sweep": sweep}
+    emit(line, args.out)
+    return 0
+
+
+def run_adjoint_workload(args):
+    """Config 5: 128^3 shear layer, fixed dt 2e-4, 100 steps, loss = mean squared
+    density difference to a seeded +-5% perturbation; gradient w.r.t. the five
+    initial conserved fields by the hand-written adjoint (sqrt(N) checkpoints),
+    checked by central differences (FP64 runs) on 32 random cells."""
+    import numpy as np
+    torch, tg, dev = _gpu_setup()
+    from tinyfluids_gb300 import adjoint as A
+    n, K, dt = 128, (args.steps if args.steps != 200 else 100), 2e-4
+    W, dx = tg.shear_layer(n, seed=0, device=dev)
+    U0 = tg.conserved_state_from_primitive(W, GAMMA)
+    g = torch.Generator(device="cpu").manual_seed(1)
+    noise = (torch.rand(W.shape[1:], generator=g) * 2 - 1).to(dev)
+    rho_t = W[0] * (1 + 0.05 * noise)
+
+    def grad(U):
+        U = U.clone().requires_grad_(True)
+        loss = A.density_mse_loss(U, rho_t.to(U.dtype), dx, dt, GAMMA, K)
+        loss.backward()
+        return U.grad, float(loss)
+
+    grad(U0)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g32, loss32 = grad(U0)
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    U64 = U0.double()
+    g64, loss64 = grad(U64)
+    rng = np.random.default_rng(2)
+    errs32, errs64 = [], []
+    scale = float(g64.abs().max())
+    with torch.no_grad():
+        for _ in range(32):
+            f = int(rng.integers(5))
+            i, j, k = (int(v) for v in rng.integers(n, size=3))
+            h = 1e-6 * max(1.0, abs(float(U64[f, i, j, k])))
+            Up, Um = U64.clone(), U64.clone()
+            Up[f, i, j, k] += h
+            Um[f, i, j, k] -= h
+            fd = (float(A.density_mse_loss(Up, rho_t.double(), dx, dt, GAMMA, K))
+                  - float(A.density_mse_loss(Um, rho_t.double(), dx, dt, GAMMA, K))) / (2 * h)
+            errs64.append(abs(fd - float(g64[f, i, j, k])) / scale)
+            errs32.append(abs(fd - float(g32[f, i, j, k])) / scale)
+    line = {"metric": "adjoint gradient, 128^3 x 100 fixed-dt steps", "value": t_grad,
+            "unit": "s per loss+gradient", "higher_is_better": False, "n_gpus": 1,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "shear layer 128^3, dt=2e-4, 100 steps, sqrt(N) checkpoints"},
+            "loss_f32": loss32, "loss_f64": loss64,
+            "fd_check": {"cells": 32, "max_err_f64_adjoint": max(errs64),
+                         "max_err_f32_adjoint": max(errs32),
+                         "relative_to": "max |dL/dU0| (FP64)"},
+            "gcell_updates_per_s_fwd_bwd": n ** 3 * K / t_grad / 1e9}
+    emit(line, args.out)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch_workload(args)
+    if args.workload == "serve":
+        return run_serve_workload(args)
+    if args.workload == "adjoint":
+        return run_adjoint_workload(args)
     return run_gpu(args)
 
 

@@ -67,7 +67,8 @@ typedef struct tf_ctl {
   int reserved[5];
 } tf_ctl;
 
-/* Tile shape of the fused step kernel; NULL = built-in heuristic. */
+/* Tile shape of the fused step kernel; NULL = built-in heuristic (16 rows,
+ * lx for about eight waves of resident CTAs). */
 typedef struct tf_tile_config {
   int rows;  /* grid rows per tile incl. the 1-cell ring: 8, 16, 32 or 34 (rows/2 warps) */
   int lx;    /* x planes per CTA (>= 1) */
@@ -122,6 +123,53 @@ int tf_time_integration(const float *W_in, float *W_out, float *work, tf_ctl *ct
 int tf_evolve_along_axis(const float *W_in, float *W_out, int nx, int ny, int nz, float dx,
                          float dt_host, const float *dt_dev, float gamma, int axis,
                          unsigned flags, void *stream);
+
+/* ---- the reference's building blocks (exact op order) ----
+ * vel is the reference's flux_direction_index (1 = x, 2 = y, 3 = z).
+ * Left/right states are full [5][ncells] arrays (the reference passes
+ * roll(W, +1, axis) and W). */
+
+/* fluid.py:106-117 speed_of_sound: c = sqrt(gamma*p/rho), n values. */
+int tf_speed_of_sound(const float *rho, const float *p, float *c, long long n, float gamma,
+                      void *stream);
+
+/* fluid.py:208-259 _euler_flux along vel. */
+int tf_euler_flux(const float *W, float *F, long long ncells, float gamma, int vel, void *stream);
+
+/* fluid.py:121-160 get_wave_speeds: S- and S+ per interface. */
+int tf_wave_speeds(const float *WL, const float *WR, float *s_minus, float *s_plus,
+                   long long ncells, float gamma, int vel, void *stream);
+
+/* fluid.py:164-195 get_max_wave_speeds: max(max|S+|, max|S-|) into
+ * ctl->max_speed (ctl is reset first). */
+int tf_max_wave_speeds(const float *WL, const float *WR, long long ncells, float gamma, int vel,
+                       tf_ctl *ctl, void *stream);
+
+/* fluid.py:263-305 _hll_solver: HLL flux of each (left, right) pair. */
+int tf_hll_flux(const float *WL, const float *WR, float *F, long long ncells, float gamma,
+                int vel, void *stream);
+
+/* fluid.py:335-413 open boundaries with num_ghost_cells ghost cells, on the
+ * axes whose bits (1 = x, 2 = y, 4 = z) are set in lo_axes (left boundary)
+ * and hi_axes (right boundary); _open_boundaries is lo = hi = 7. */
+int tf_open_boundaries(const float *W, float *out, int nx, int ny, int nz, int num_ghost_cells,
+                       unsigned lo_axes, unsigned hi_axes, void *stream);
+
+/* ---- adjoint of the fixed-dt step (conserved variables) ----
+ * Adjoint of one periodic sweep along axis (0..2) of the fast scheme:
+ * given the sweep's input U (conserved) and lam_out = dL/dU', writes
+ * lam_in = dL/dU.  A step's adjoint is axis 2, 1, 0 in turn, each with the
+ * input state of that forward sweep.  No reference counterpart (the
+ * reference relies on JAX autodiff of fluid.py). */
+int tf_adjoint_sweep(const float *U, const float *lam_out, float *lam_in, int nx, int ny, int nz,
+                     float dx, float dt, float gamma, int axis, void *stream);
+int tf_adjoint_sweep_f64(const double *U, const double *lam_out, double *lam_in, int nx, int ny,
+                         int nz, double dx, double dt, double gamma, int axis, void *stream);
+
+/* FP64 forward sweep of the same scheme on conserved states (for the
+ * finite-difference check of the adjoint). */
+int tf_sweep_conserved_f64(const double *U, double *out, int nx, int ny, int nz, double dx,
+                           double dt, double gamma, int axis, void *stream);
 
 /* Largest grid (nx*ny*nz cells) tf_time_integration_noalloc accepts. */
 #define TF_NOALLOC_MAX_CELLS (1 << 18)

@@ -1,0 +1,91 @@
+"""The hand-written adjoint of the fixed-dt step.
+
+Checked against (1) torch.autograd of the FP64 restatement of the reference
+step (oracle/torch_ref.py, the stand-in for JAX's gradient), (2) central
+finite differences of the FP64 forward run, and (3) itself across checkpoint
+segment lengths; the float32 adjoint is checked against the float64 one."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import torch_ref
+from tinyfluids_gb300 import adjoint as A
+
+pytestmark = pytest.mark.gpu
+GAMMA = 5.0 / 3.0
+
+
+def shear_conserved(tg, n, seed, dtype=torch.float64):
+    W, dx = tg.shear_layer(n, seed=seed, amplitude=0.05)
+    U = tg.conserved_state_from_primitive(W, GAMMA)
+    return U.to(dtype), dx
+
+
+def target_from(U, seed):
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    noise = (torch.rand(U.shape[1:], generator=g, dtype=torch.float64) * 2 - 1).to(U.device)
+    return (U[0] * (1 + 0.05 * noise)).to(U.dtype)
+
+
+def grad_of(loss_fn, U0):
+    U = U0.clone().requires_grad_(True)
+    loss = loss_fn(U)
+    loss.backward()
+    return U.grad, float(loss)
+
+
+def test_adjoint_matches_autograd_of_reference_restatement(tg):
+    U0, _ = shear_conserved(tg, 12, 1)
+    U0 = U0[:, :12, :10, :8].contiguous()
+    rho_t = target_from(U0, 2)
+    dx, dt, steps = 1 / 12, 2e-3, 3
+    g_ours, l_ours = grad_of(lambda U: A.density_mse_loss(U, rho_t, dx, dt, GAMMA, steps), U0)
+    g_ref, l_ref = grad_of(lambda U: torch_ref.density_mse_loss(U.cpu(), rho_t.cpu(), dx, dt,
+                                                                GAMMA, steps), U0)
+    assert abs(l_ours - l_ref) <= 1e-12 * abs(l_ref)
+    err = float((g_ours.cpu() - g_ref.cpu()).abs().max() / g_ref.abs().max())
+    assert err < 1e-9, err
+
+
+def test_adjoint_matches_central_differences(tg):
+    U0, dx = shear_conserved(tg, 16, 3)
+    rho_t = target_from(U0, 4)
+    dt, steps = 2e-3, 6
+    g, _ = grad_of(lambda U: A.density_mse_loss(U, rho_t, dx, dt, GAMMA, steps), U0)
+    rng = np.random.default_rng(5)
+    with torch.no_grad():
+        for _ in range(12):
+            f, i, j, k = (int(rng.integers(5)), *(int(v) for v in rng.integers(16, size=3)))
+            h = 1e-6 * max(1.0, abs(float(U0[f, i, j, k])))
+            Up, Um = U0.clone(), U0.clone()
+            Up[f, i, j, k] += h
+            Um[f, i, j, k] -= h
+            fd = (float(A.density_mse_loss(Up, rho_t, dx, dt, GAMMA, steps))
+                  - float(A.density_mse_loss(Um, rho_t, dx, dt, GAMMA, steps))) / (2 * h)
+            ad = float(g[f, i, j, k])
+            assert abs(fd - ad) <= 1e-6 * max(abs(ad), 1e-3 * float(g.abs().max())), (f, fd, ad)
+
+
+def test_checkpoint_segments_give_identical_gradients(tg):
+    U0, dx = shear_conserved(tg, 20, 6, torch.float32)
+    rho_t = target_from(U0, 7)
+    grads = [grad_of(lambda U: A.density_mse_loss(U, rho_t, dx, 1e-3, GAMMA, 7, seg), U0)[0]
+             for seg in (1, 3, None, 7)]
+    for g in grads[1:]:
+        assert torch.equal(g, grads[0])
+
+
+def test_float32_adjoint_close_to_float64(tg):
+    U64, dx = shear_conserved(tg, 24, 8)
+    rho_t = target_from(U64, 9)
+    g64, _ = grad_of(lambda U: A.density_mse_loss(U, rho_t, dx, 2e-3, GAMMA, 10), U64)
+    g32, _ = grad_of(lambda U: A.density_mse_loss(U, rho_t.float(), dx, 2e-3, GAMMA, 10),
+                     U64.float())
+    err = float((g32.double() - g64).abs().max() / g64.abs().max())
+    assert err < 1e-3, err
+
+
+def test_zero_steps_is_identity(tg):
+    U0, dx = shear_conserved(tg, 8, 1, torch.float32)
+    g, _ = grad_of(lambda U: A.fixed_dt_run(U, dx, 1e-3, GAMMA, 0).sum(), U0)
+    assert torch.equal(g, torch.ones_like(U0))

@@ -65,6 +65,18 @@ SIGNATURES = {
     "tf_batch_run": (c_int, [vp, c_int, c_int, vp]),
     "tf_batch_error": (c_int, [vp, vp, vp]),
     "tf_batch_release": (c_int, [vp]),
+    "tf_speed_of_sound": (c_int, [vp, vp, vp, c_ll, c_float, vp]),
+    "tf_euler_flux": (c_int, [vp, vp, c_ll, c_float, c_int, vp]),
+    "tf_wave_speeds": (c_int, [vp, vp, vp, vp, c_ll, c_float, c_int, vp]),
+    "tf_max_wave_speeds": (c_int, [vp, vp, c_ll, c_float, c_int, vp, vp]),
+    "tf_hll_flux": (c_int, [vp, vp, vp, c_ll, c_float, c_int, vp]),
+    "tf_open_boundaries": (c_int, [vp, vp, c_int, c_int, c_int, c_int, c_uint, c_uint, vp]),
+    "tf_adjoint_sweep": (c_int, [vp, vp, vp, c_int, c_int, c_int, c_float, c_float, c_float,
+                                 c_int, vp]),
+    "tf_adjoint_sweep_f64": (c_int, [vp, vp, vp, c_int, c_int, c_int, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_double, c_int, vp]),
+    "tf_sweep_conserved_f64": (c_int, [vp, vp, c_int, c_int, c_int, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_double, c_int, vp]),
     "tf_ics_injection_cube": (c_int, [vp, c_int, c_int, vp]),
     "tf_ics_overpressure": (c_int, [vp, c_int, c_ull, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]),

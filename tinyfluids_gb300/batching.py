@@ -13,6 +13,7 @@ from __future__ import annotations
 import ctypes
 import math
 from dataclasses import dataclass
+from dataclasses import replace as _replace
 
 import torch
 
@@ -41,8 +42,8 @@ class Batch:
     """A prepared batch; ``run()`` advances every instance and returns the
     final states (new tensors, inputs untouched)."""
 
-    def __init__(self, specs, *, rows=32, exact=None, persistent=True, ctas_per_sm=0,
-                 wait_limit=0, capture_graph=False, steps=None):
+    def __init__(self, specs, *, rows=16, exact=None, persistent=True, ctas_per_sm=0,
+                 wait_limit=0, capture_graph=False, steps=None, autotune=False):
         self._closed = True
         if not specs:
             raise ValueError("a batch needs at least one instance")
@@ -65,6 +66,12 @@ class Batch:
                                  "(an upper bound on their step count)")
             steps = max(caps)
         self.steps = int(steps)
+        if autotune:
+            from . import autotune as _at
+            rows, lxs = _at.tune_batch([tuple(sp.state.shape[1:]) for sp in self.specs],
+                                       exact=self.exact, device=dev)
+            self.specs = [sp if sp.lx else _replace(sp, lx=lx) for sp, lx in zip(self.specs, lxs)]
+        self.rows = int(rows)
         with torch.cuda.device(dev):
             self.inputs = [check_state(sp.state) for sp in self.specs]
             self.outputs = [sp.out if sp.out is not None else torch.empty_like(W)

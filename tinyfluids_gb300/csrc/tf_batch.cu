@@ -49,7 +49,7 @@ struct BatchHeader {
 
 struct BatchPlan {  // host mirror of a prepared workspace
   int count = 0;
-  int rows = 32;
+  int rows = 16;
   int exact = 0;
   int persistent = 1;
   int ctas_per_sm = 0;

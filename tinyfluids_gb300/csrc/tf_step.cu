@@ -219,9 +219,9 @@ static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int
   g.tiles_z = (nz + kTileZ - 1) / kTileZ;
   g.tiles_y = (ny + (rows - 2) - 1) / (rows - 2);
   if (lx <= 0) {
-    // enough CTAs for ~8 waves at one CTA per SM, chunks of >= 8 planes
+    // enough CTAs for ~8 waves of resident CTAs, chunks of >= 8 planes
     long long tiles_yz = (long long)g.tiles_z * g.tiles_y;
-    long long want = 8LL * sm_count();
+    long long want = 8LL * sm_count() * min_ctas_per_sm(rows / 2);
     long long tx = (want + tiles_yz - 1) / tiles_yz;
     long long max_tx = nx / 8 > 0 ? nx / 8 : 1;
     if (tx > max_tx) tx = max_tx;
@@ -235,7 +235,7 @@ static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int
 }
 
 static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx) {
-  *rows = 32;
+  *rows = 16;  // two CTAs per SM interleave their barrier phases (measured best at 512^3)
   *lx = 0;
   if (tile) {
     if (!valid_tile_rows(tile->rows))

@@ -136,6 +136,112 @@ def primitive_state_from_conserved(conserved_state, gamma):
 
 
 # ---------------------------------------------------------------------------
+# fluid.py:105-413 -- the reference's building blocks (reference op order)
+# ---------------------------------------------------------------------------
+def _field(x, name):
+    if not isinstance(x, torch.Tensor) or x.dtype != torch.float32 or not x.is_cuda:
+        raise TypeError(f"{name} must be a float32 CUDA tensor")
+    return x.contiguous()
+
+
+def _pair(left, right):
+    L = check_state(left, "primitives_left")
+    R = check_state(right, "primitives_right")
+    if L.shape != R.shape or L.device != R.device:
+        raise TypeError("primitives_left and primitives_right must match")
+    return L, R
+
+
+def _vel(i):
+    i = int(i)
+    if i not in (VELOCITY_X_INDEX, VELOCITY_Y_INDEX, VELOCITY_Z_INDEX):
+        raise ValueError("flux_direction_index must be 1, 2 or 3")
+    return i
+
+
+def speed_of_sound(rho, p, gamma):
+    """fluid.py:106-117: sqrt(gamma*p/rho) elementwise."""
+    rho, p = _field(rho, "rho"), _field(p, "p")
+    if rho.shape != p.shape:
+        raise TypeError("rho and p must have the same shape")
+    with torch.cuda.device(rho.device):
+        c = torch.empty_like(rho)
+        _lib.call("tf_speed_of_sound", rho.data_ptr(), p.data_ptr(), c.data_ptr(), rho.numel(),
+                  _scalar(gamma, "gamma"), _stream(rho))
+    return c
+
+
+def get_wave_speeds(primitives_left, primitives_right, gamma, flux_direction_index):
+    """fluid.py:121-160: (S-, S+) = (min(uL-cL, uR-cR, 0), max(uL+cL, uR+cR, 0))."""
+    L, R = _pair(primitives_left, primitives_right)
+    with torch.cuda.device(L.device):
+        sm = torch.empty_like(L[0])
+        sp = torch.empty_like(L[0])
+        _lib.call("tf_wave_speeds", L.data_ptr(), R.data_ptr(), sm.data_ptr(), sp.data_ptr(),
+                  L[0].numel(), _scalar(gamma, "gamma"), _vel(flux_direction_index), _stream(L))
+    return sm, sp
+
+
+def get_max_wave_speeds(primitives_left, primitives_right, gamma, flux_direction_index):
+    """fluid.py:164-195: max(max|S+|, max|S-|) as a 0-d CUDA tensor."""
+    L, R = _pair(primitives_left, primitives_right)
+    with torch.cuda.device(L.device):
+        ctl = new_ctl(L.device)
+        _lib.call("tf_max_wave_speeds", L.data_ptr(), R.data_ptr(), L[0].numel(),
+                  _scalar(gamma, "gamma"), _vel(flux_direction_index), ctl.data_ptr(), _stream(L))
+    return ctl.view(torch.float32)[CTL_MAXSPEED].clone()
+
+
+def _euler_flux(primitive_state, gamma, flux_direction_index):
+    """fluid.py:208-259: the physical flux along the given velocity index."""
+    W = check_state(primitive_state)
+    with torch.cuda.device(W.device):
+        F = torch.empty_like(W)
+        _lib.call("tf_euler_flux", W.data_ptr(), F.data_ptr(), W[0].numel(),
+                  _scalar(gamma, "gamma"), _vel(flux_direction_index), _stream(W))
+    return F
+
+
+def _hll_solver(primitives_left, primitives_right, gamma, flux_direction_index):
+    """fluid.py:263-305: the HLL flux of every (left, right) pair."""
+    L, R = _pair(primitives_left, primitives_right)
+    with torch.cuda.device(L.device):
+        F = torch.empty_like(L)
+        _lib.call("tf_hll_flux", L.data_ptr(), R.data_ptr(), F.data_ptr(), L[0].numel(),
+                  _scalar(gamma, "gamma"), _vel(flux_direction_index), _stream(L))
+    return F
+
+
+def _open_boundary_call(W, num_ghost_cells, lo, hi):
+    W = check_state(W)
+    _, nx, ny, nz = W.shape
+    with torch.cuda.device(W.device):
+        out = torch.empty_like(W)
+        _lib.call("tf_open_boundaries", W.data_ptr(), out.data_ptr(), nx, ny, nz,
+                  int(num_ghost_cells), lo, hi, _stream(W))
+    return out
+
+
+def _open_boundaries(primitive_state, num_ghost_cells):
+    """fluid.py:384-413: zero-gradient ghost cells on every face (x, y, z)."""
+    return _open_boundary_call(primitive_state, num_ghost_cells, 7, 7)
+
+
+def _open_left_boundary(primitive_state, num_ghost_cells, axis):
+    """fluid.py:358-379 (axis X_AXIS, Y_AXIS or Z_AXIS)."""
+    if axis not in (X_AXIS, Y_AXIS, Z_AXIS):
+        raise ValueError("axis must be X_AXIS, Y_AXIS or Z_AXIS")
+    return _open_boundary_call(primitive_state, num_ghost_cells, 1 << (axis - 1), 0)
+
+
+def _open_right_boundary(primitive_state, num_ghost_cells, axis):
+    """fluid.py:335-354 (axis X_AXIS, Y_AXIS or Z_AXIS)."""
+    if axis not in (X_AXIS, Y_AXIS, Z_AXIS):
+        raise ValueError("axis must be X_AXIS, Y_AXIS or Z_AXIS")
+    return _open_boundary_call(primitive_state, num_ghost_cells, 0, 1 << (axis - 1))
+
+
+# ---------------------------------------------------------------------------
 # fluid.py:427-504
 # ---------------------------------------------------------------------------
 def _cfl_time_step(primitive_state, grid_spacing, gamma, C_CFL=0.4):
@@ -165,7 +271,7 @@ def _evolve_state(primitive_state, grid_spacing, dt, gamma, handle_boundaries=Fa
     with torch.cuda.device(W.device):
         out = torch.empty_like(W)
         dt_host, dt_dev, keep = _dt_args(dt, W.device)
-        tc = _tile_arg(tile)
+        tc = _tile_arg(tile, W, exact)
         _lib.call("tf_evolve_state", W.data_ptr(), out.data_ptr(), nx, ny, nz,
                   float(grid_spacing), dt_host, dt_dev, _scalar(gamma, "gamma"),
                   _flags(handle_boundaries, exact), tc, _stream(W))
@@ -197,8 +303,16 @@ def _evolve_state_along_axis(primitive_state, grid_spacing, dt, gamma, axis, *,
     return out
 
 
-def _tile_arg(tile):
+def _tile_arg(tile, state=None, exact=None):
+    """tf_tile_config for `tile`: None (built-in heuristic), (rows, lx), or
+    "auto" (the autotuner's measured best for this grid shape)."""
     if tile is None:
         return None
+    if isinstance(tile, str):
+        if tile != "auto" or state is None:
+            raise ValueError("tile must be None, (rows, lx) or 'auto'")
+        from . import autotune
+        ex = _EXACT if exact is None else bool(exact)
+        tile = autotune.tuned_tile(tuple(state.shape[1:]), exact=ex, device=state.device)
     rows, lx = tile
     return ctypes.byref(_lib.TileConfig(int(rows), int(lx)))

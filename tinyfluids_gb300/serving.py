@@ -78,7 +78,7 @@ class _Active:
 class Server:
     """Admits requests by free HBM budget and advances all admitted ones together."""
 
-    def __init__(self, hbm_budget=120e9, device=None, tick_steps=16, rows=32,
+    def __init__(self, hbm_budget=120e9, device=None, tick_steps=16, rows=16,
                  cfl=0.4, keep_states=False, max_active=4096):
         self.device = torch.device(device if device is not None else "cuda")
         self.budget = int(hbm_budget)

@@ -62,7 +62,7 @@ def _run(primitive_state, grid_spacing, gamma, t_final, max_steps, fixed_dt,
         _lib.call("tf_time_integration", W.data_ptr(), out.data_ptr(), work.data_ptr(),
                   ctl.data_ptr(), nx, ny, nz, float(grid_spacing), float(t_final),
                   _scalar(gamma, "gamma"), _scalar(C_CFL, "C_CFL"), int(max_steps),
-                  float(fixed_dt), _flags(handle_boundaries, exact), _tile_arg(tile),
+                  float(fixed_dt), _flags(handle_boundaries, exact), _tile_arg(tile, W, exact),
                   _lib.ctypes.byref(it) if wait else None, _stream(W))
     return out, (it.value if wait else None), ctl
 
