@@ -24,8 +24,9 @@ c_char_p = ctypes.c_char_p
 
 
 class TileConfig(ctypes.Structure):
-    """tf_tile_config: warps per CTA (8 or 16, incl. 2 halo rows) and x planes per CTA."""
-    _fields_ = [("rows", c_int), ("lx", c_int)]
+    """tf_tile_config: tile rows (8, 16, 32, 34), x planes per CTA, plane loader
+    (0 auto, 1 per-thread loads, 2 TMA-staged)."""
+    _fields_ = [("rows", c_int), ("lx", c_int), ("loader", c_int)]
 
 
 class Instance(ctypes.Structure):

@@ -71,168 +71,393 @@ __device__ __forceinline__ void shfl_up_cell2(const Cell2& in, Cell2& out) {
   out.c.y = __shfl_up_sync(0xffffffffu, in.c.y, 1);
 }
 
-// One CTA-tile of the fused step.  Returns this thread's running maximum of
-// the stored cells' wave speeds (0 for threads that store nothing).
-// COHERENT selects L2-only loads (ld.global.cg) for kernels that read data
-// other CTAs wrote earlier in the same launch (the persistent batch kernel);
-// otherwise loads use the read-only path.
+// Per-thread context of one tile: store targets and the running CFL speed.
+struct TileOut {
+  float* dst;
+  size_t plane, vstride, dcol_a, dcol_b;
+  bool store_a, store_b;
+  float wmax;
+};
+
+// One plane of the fused step for the thread's pair of cells: the x sweep
+// from registers (cur = plane x, pf = plane x+1, fm = flux at x-1/2), then
+// the y and z sweeps, the store and the CFL epilogue.  `consumed()` runs as
+// soon as pf has been read (the register-prefetch loader refills pf there);
+// `after_sync()` runs after the plane's first CTA barrier, when every thread
+// has read plane x+1 (the TMA loader refills its stage there) and returns
+// true if the CTA must stop (a bounded wait gave up).
+template <class P, int NWP, class Consumed, class AfterSync>
+__device__ __forceinline__ bool plane_update(int x, V2 pf[5], Cell2& cur, V2 fm[5],
+                                             const StepConsts<float>& K, FusedSmem<NWP>& sm,
+                                             TileOut& o, Consumed consumed, AfterSync after_sync) {
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  V2 s[5];
+  Cell2 nxt;
+  P::to_state(pf, s, K);
+  P::template derive<1>(s, nxt, K);
+  consumed();
+  V2 fp[5];
+  P::hll(cur, nxt, fp);  // face x + 1/2
+  V2 s1[5];
+  P::update(cur, fm, fp, s1, K);
+
+  // ---- y sweep ----
+  Cell2 cy;
+  P::template derive<2>(s1, cy, K);
+  sm.cy[0][w][lane] = make_float4(cy.U[0].y, cy.U[1].y, cy.U[2].y, cy.U[3].y);
+  sm.cy[1][w][lane] = make_float4(cy.U[4].y, cy.F[0].y, cy.F[1].y, cy.F[2].y);
+  sm.cy[2][w][lane] = make_float4(cy.F[3].y, cy.F[4].y, cy.u.y, cy.c.y);
+  const bool stop = after_sync();
+  // L = (cell above the pair, upper cell), R = (upper cell, lower cell):
+  // faces (ya - 1/2, ya + 1/2).  Warp 0 has no cell above (its upper row
+  // is the ring); it uses its own upper cell, and that face is never used.
+  Cell2 L;
+  {
+    float4 a, b, d;
+    if (w >= 1) {
+      a = sm.cy[0][w - 1][lane];
+      b = sm.cy[1][w - 1][lane];
+      d = sm.cy[2][w - 1][lane];
+    } else {
+      a = make_float4(cy.U[0].x, cy.U[1].x, cy.U[2].x, cy.U[3].x);
+      b = make_float4(cy.U[4].x, cy.F[0].x, cy.F[1].x, cy.F[2].x);
+      d = make_float4(cy.F[3].x, cy.F[4].x, cy.u.x, cy.c.x);
+    }
+    L.U[0] = v2(a.x, cy.U[0].x); L.U[1] = v2(a.y, cy.U[1].x);
+    L.U[2] = v2(a.z, cy.U[2].x); L.U[3] = v2(a.w, cy.U[3].x);
+    L.U[4] = v2(b.x, cy.U[4].x); L.F[0] = v2(b.y, cy.F[0].x);
+    L.F[1] = v2(b.z, cy.F[1].x); L.F[2] = v2(b.w, cy.F[2].x);
+    L.F[3] = v2(d.x, cy.F[3].x); L.F[4] = v2(d.y, cy.F[4].x);
+    L.u = v2(d.z, cy.u.x);       L.c = v2(d.w, cy.c.x);
+  }
+  V2 fy[5];
+  P::hll(L, cy, fy);
+  sm.fy4[w][lane] = make_float4(fy[0].x, fy[1].x, fy[2].x, fy[3].x);
+  sm.fy1[w][lane] = fy[4].x;
+  __syncthreads();
+  // face below the pair = the next warp's face above its pair; the last
+  // warp's lower row is the ring and takes its own value (unused)
+  V2 fyh[5];
+  {
+    float4 f4;
+    float f1;
+    if (w <= NWP - 2) {
+      f4 = sm.fy4[w + 1][lane];
+      f1 = sm.fy1[w + 1][lane];
+    } else {
+      f4 = make_float4(fy[0].x, fy[1].x, fy[2].x, fy[3].x);
+      f1 = fy[4].x;
+    }
+    fyh[0] = v2(fy[0].y, f4.x);
+    fyh[1] = v2(fy[1].y, f4.y);
+    fyh[2] = v2(fy[2].y, f4.z);
+    fyh[3] = v2(fy[3].y, f4.w);
+    fyh[4] = v2(fy[4].y, f1);
+  }
+  V2 s2[5];
+  P::update(cy, fy, fyh, s2, K);
+
+  // ---- z sweep ----
+  Cell2 cz, nb;
+  P::template derive<3>(s2, cz, K);
+  shfl_up_cell2(cz, nb);
+  V2 fzl[5], fzh[5];
+  P::hll(nb, cz, fzl);  // faces between lanes l-1 and l, both rows
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    fzh[i].x = __shfl_down_sync(0xffffffffu, fzl[i].x, 1);
+    fzh[i].y = __shfl_down_sync(0xffffffffu, fzl[i].y, 1);
+  }
+  V2 s3[5], wo[5];
+  P::update(cz, fzl, fzh, s3, K);
+  const V2 sp = P::finish(s3, wo, K);
+  float* q = o.dst + (size_t)x * o.plane;
+  if (o.store_a) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) q[i * o.vstride + o.dcol_a] = wo[i].x;
+    o.wmax = speed_max(o.wmax, sp.x);
+  }
+  if (o.store_b) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) q[i * o.vstride + o.dcol_b] = wo[i].y;
+    o.wmax = speed_max(o.wmax, sp.y);
+  }
+#pragma unroll
+  for (int i = 0; i < 5; ++i) fm[i] = fp[i];
+  cur = nxt;
+  return stop;
+}
+
+// Geometry of the thread's two cells within a tile.
+struct TileCols {
+  int x0, x_end, z, ya, yb;
+  size_t col_a, col_b;  // source columns (wrapped / clamped)
+};
+
+template <int NWP>
+__device__ __forceinline__ TileCols tile_cols(const FusedGeom& G, int tz, int ty, int tx,
+                                              const float* src, float* dst, TileOut& o) {
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const bool open = G.open_bc != 0;
+  TileCols t;
+  const int z0 = tz * kTileZ, y0 = ty * tile_rows_out(NWP);
+  t.x0 = tx * G.lx;
+  t.x_end = min(t.x0 + G.lx, G.nx);
+  t.z = z0 - 1 + lane;
+  t.ya = y0 - 1 + 2 * w;
+  t.yb = t.ya + 1;
+  const int zs = src_index(t.z, G.nz, open);
+  t.col_a = (size_t)src_index(t.ya, G.ny, open) * G.nz + zs;
+  t.col_b = (size_t)src_index(t.yb, G.ny, open) * G.nz + zs;
+  o.dst = dst;
+  o.plane = (size_t)G.ny * G.nz;
+  o.vstride = o.plane * G.nx;
+  const bool store_lane = lane >= 1 && lane <= kTileLanes - 2 && t.z < G.nz;
+  o.store_a = store_lane && w >= 1 && t.ya < G.ny;
+  o.store_b = store_lane && w <= NWP - 2 && t.yb < G.ny;
+  o.dcol_a = o.store_a ? (size_t)t.ya * G.nz + t.z : 0;
+  o.dcol_b = o.store_b ? (size_t)t.yb * G.nz + t.z : 0;
+  o.wmax = 0.f;
+  return t;
+}
+
+// One CTA-tile of the fused step, planes loaded by each thread with
+// register prefetch.  Returns this thread's running maximum of the stored
+// cells' wave speeds (0 for threads that store nothing).  COHERENT selects
+// L2-only loads (ld.global.cg) for kernels that read data other CTAs wrote
+// earlier in the same launch (the persistent batch kernel); otherwise loads
+// use the read-only path.
 template <class P, int NWP, bool COHERENT = false>
 __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float* __restrict__ dst,
                                             const FusedGeom& G, int tz, int ty, int tx,
                                             const StepConsts<float>& K, FusedSmem<NWP>& sm) {
-  const int lane = threadIdx.x & 31;
-  const int w = threadIdx.x >> 5;
+  TileOut o;
+  const TileCols t = tile_cols<NWP>(G, tz, ty, tx, src, dst, o);
   const bool open = G.open_bc != 0;
-  const int z0 = tz * kTileZ, y0 = ty * tile_rows_out(NWP);
-  const int x0 = tx * G.lx;
-  const int x_end = min(x0 + G.lx, G.nx);
-  const int z = z0 - 1 + lane;
-  const int ya = y0 - 1 + 2 * w, yb = ya + 1;  // the thread's two rows
-  const size_t plane = (size_t)G.ny * G.nz;
-  const size_t vstride = plane * G.nx;
-  const int zs = src_index(z, G.nz, open);
-  const size_t col_a = (size_t)src_index(ya, G.ny, open) * G.nz + zs;
-  const size_t col_b = (size_t)src_index(yb, G.ny, open) * G.nz + zs;
-  const bool store_lane = lane >= 1 && lane <= kTileLanes - 2 && z < G.nz;
-  const bool store_a = store_lane && w >= 1 && ya < G.ny;
-  const bool store_b = store_lane && w <= NWP - 2 && yb < G.ny;
-  const size_t dcol_a = store_a ? (size_t)ya * G.nz + z : 0;
-  const size_t dcol_b = store_b ? (size_t)yb * G.nz + z : 0;
-
   auto load = [&](int x, V2 v[5]) {
-    const float* p = src + (size_t)src_index(x, G.nx, open) * plane;
+    const float* p = src + (size_t)src_index(x, G.nx, open) * o.plane;
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
-      const float* q = p + i * vstride;
-      v[i].x = COHERENT ? __ldcg(q + col_a) : __ldg(q + col_a);
-      v[i].y = COHERENT ? __ldcg(q + col_b) : __ldg(q + col_b);
+      const float* q = p + i * o.vstride;
+      v[i].x = COHERENT ? __ldcg(q + t.col_a) : __ldg(q + t.col_a);
+      v[i].y = COHERENT ? __ldcg(q + t.col_b) : __ldg(q + t.col_b);
     }
   };
-
-  float wmax = 0.f;
   Cell2 cur;
   V2 fm[5];
   V2 pa[5], pb[5];
   {
     V2 w0[5], s[5];
-    load(x0 - 1, w0);
-    load(x0, pa);
-    load(x0 + 1, pb);
+    load(t.x0 - 1, w0);
+    load(t.x0, pa);
+    load(t.x0 + 1, pb);
     P::to_state(w0, s, K);
     P::template derive<1>(s, cur, K);
     Cell2 nx_;
     P::to_state(pa, s, K);
     P::template derive<1>(s, nx_, K);
-    if (x0 + 2 <= x_end) load(x0 + 2, pa);
+    if (t.x0 + 2 <= t.x_end) load(t.x0 + 2, pa);
     P::hll(cur, nx_, fm);  // flux at face x0 - 1/2
     cur = nx_;
   }
-
-  // One plane: x sweep from registers, then y and z sweeps, store, epilogue.
+  auto sync_only = []() {
+    __syncthreads();
+    return false;
+  };
+  // Two planes per trip so the two prefetch buffers alternate without moves;
   // `pf` holds plane x+1 on entry and receives plane x+3.
-  auto plane_step = [&](int x, V2 pf[5]) {
-    V2 s[5];
-    Cell2 nxt;
-    P::to_state(pf, s, K);
-    P::template derive<1>(s, nxt, K);
-    if (x + 3 <= x_end) load(x + 3, pf);
-    V2 fp[5];
-    P::hll(cur, nxt, fp);  // face x + 1/2
-    V2 s1[5];
-    P::update(cur, fm, fp, s1, K);
+  for (int x = t.x0; x < t.x_end; x += 2) {
+    plane_update<P, NWP>(x, pb, cur, fm, K, sm, o,
+                         [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); }, sync_only);
+    if (x + 1 < t.x_end)
+      plane_update<P, NWP>(x + 1, pa, cur, fm, K, sm, o,
+                           [&]() { if (x + 4 <= t.x_end) load(x + 4, pa); }, sync_only);
+  }
+  return o.wmax;
+}
 
-    // ---- y sweep ----
-    Cell2 cy;
-    P::template derive<2>(s1, cy, K);
-    sm.cy[0][w][lane] = make_float4(cy.U[0].y, cy.U[1].y, cy.U[2].y, cy.U[3].y);
-    sm.cy[1][w][lane] = make_float4(cy.U[4].y, cy.F[0].y, cy.F[1].y, cy.F[2].y);
-    sm.cy[2][w][lane] = make_float4(cy.F[3].y, cy.F[4].y, cy.u.y, cy.c.y);
-    __syncthreads();
-    // L = (cell above the pair, upper cell), R = (upper cell, lower cell):
-    // faces (ya - 1/2, ya + 1/2).  Warp 0 has no cell above (its upper row
-    // is the ring); it uses its own upper cell, and that face is never used.
-    Cell2 L;
-    {
-      float4 a, b, d;
-      if (w >= 1) {
-        a = sm.cy[0][w - 1][lane];
-        b = sm.cy[1][w - 1][lane];
-        d = sm.cy[2][w - 1][lane];
-      } else {
-        a = make_float4(cy.U[0].x, cy.U[1].x, cy.U[2].x, cy.U[3].x);
-        b = make_float4(cy.U[4].x, cy.F[0].x, cy.F[1].x, cy.F[2].x);
-        d = make_float4(cy.F[3].x, cy.F[4].x, cy.u.x, cy.c.x);
-      }
-      L.U[0] = v2(a.x, cy.U[0].x); L.U[1] = v2(a.y, cy.U[1].x);
-      L.U[2] = v2(a.z, cy.U[2].x); L.U[3] = v2(a.w, cy.U[3].x);
-      L.U[4] = v2(b.x, cy.U[4].x); L.F[0] = v2(b.y, cy.F[0].x);
-      L.F[1] = v2(b.z, cy.F[1].x); L.F[2] = v2(b.w, cy.F[2].x);
-      L.F[3] = v2(d.x, cy.F[3].x); L.F[4] = v2(d.y, cy.F[4].x);
-      L.u = v2(d.z, cy.u.x);       L.c = v2(d.w, cy.c.x);
-    }
-    V2 fy[5];
-    P::hll(L, cy, fy);
-    sm.fy4[w][lane] = make_float4(fy[0].x, fy[1].x, fy[2].x, fy[3].x);
-    sm.fy1[w][lane] = fy[4].x;
-    __syncthreads();
-    // face below the pair = the next warp's face above its pair; the last
-    // warp's lower row is the ring and takes its own value (unused)
-    V2 fyh[5];
-    {
-      float4 f4;
-      float f1;
-      if (w <= NWP - 2) {
-        f4 = sm.fy4[w + 1][lane];
-        f1 = sm.fy1[w + 1][lane];
-      } else {
-        f4 = make_float4(fy[0].x, fy[1].x, fy[2].x, fy[3].x);
-        f1 = fy[4].x;
-      }
-      fyh[0] = v2(fy[0].y, f4.x);
-      fyh[1] = v2(fy[1].y, f4.y);
-      fyh[2] = v2(fy[2].y, f4.z);
-      fyh[3] = v2(fy[3].y, f4.w);
-      fyh[4] = v2(fy[4].y, f1);
-    }
-    V2 s2[5];
-    P::update(cy, fy, fyh, s2, K);
+// ---------------------------------------------------------------------------
+// TMA-staged planes
+// ---------------------------------------------------------------------------
+// One elected thread copies each x plane of the tile -- all five variables,
+// the tile's rows including the ring, and a 40-float window of z rounded
+// down to a 16-byte boundary -- from HBM into a shared-memory ring of
+// kStages stages with one cp.async.bulk.tensor per plane; an mbarrier per
+// stage signals its arrival.  Threads then read their two cells with
+// constant-offset shared loads.  The tensor copy does not wrap, so threads
+// whose source column is wrapped (periodic) or clamped (open boundaries) --
+// only in tiles on the domain edge -- read that column directly from HBM.
+constexpr int kStages = 3;
+constexpr int kBoxZ = 40;  // z window: 32 lanes + up to 3 cells of 16-byte rounding, padded
 
-    // ---- z sweep ----
-    Cell2 cz, nb;
-    P::template derive<3>(s2, cz, K);
-    shfl_up_cell2(cz, nb);
-    V2 fzl[5], fzh[5];
-    P::hll(nb, cz, fzl);  // faces between lanes l-1 and l, both rows
+__host__ __device__ constexpr size_t tma_stage_floats(int nwp) { return (size_t)5 * 2 * nwp * kBoxZ; }
+__host__ __device__ constexpr size_t tma_smem_bytes(int nwp) {
+  return kStages * tma_stage_floats(nwp) * sizeof(float);
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long tf_global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for an mbarrier phase; gives up after `limit_ns` and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  unsigned long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = tf_global_ns();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (tf_global_ns() - t0 > limit_ns) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_plane(void* dst, const void* tmap, unsigned long long* bar,
+                                               int zc, int yc, int xc) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(tmap)), "r"(zc), "r"(yc), "r"(xc), "r"(0),
+      "r"(smem_u32(bar))
+      : "memory");
+}
+
+constexpr unsigned long long kTmaWaitNs = 2000000000ull;  // 2 s per stage wait
+
+// The fused tile with TMA-staged planes.  `tmap` describes `src` as a 4D
+// tensor (z, y, x, var) with box (kBoxZ, 2*NWP, 1, 5).  Sets *timed_out (the
+// CTA stopped early because a stage never arrived) and returns the running
+// CFL speed like fused_tile.
+template <class P, int NWP>
+__device__ __forceinline__ float fused_tile_tma(const float* __restrict__ src,
+                                                float* __restrict__ dst, const void* tmap,
+                                                const FusedGeom& G, int tz, int ty, int tx,
+                                                const StepConsts<float>& K, FusedSmem<NWP>& sm,
+                                                float* stages, unsigned long long* bars,
+                                                bool* timed_out) {
+  constexpr int ROWS = 2 * NWP;
+  constexpr size_t SF = tma_stage_floats(NWP);
+  constexpr unsigned STAGE_BYTES = (unsigned)(SF * sizeof(float));
+  const int w = threadIdx.x >> 5;
+  const bool open = G.open_bc != 0;
+  TileOut o;
+  const TileCols t = tile_cols<NWP>(G, tz, ty, tx, src, dst, o);
+  const int z0 = tz * kTileZ, y0 = ty * tile_rows_out(NWP);
+  const int zb = (z0 - 1) >= 0 ? ((z0 - 1) & ~3) : -4;  // 16-byte aligned window start
+  const int scol = t.z - zb;                              // 0..34
+  // a cell whose source column is not its own (wrapped or clamped) reads HBM
+  const bool direct_a = t.col_a != (size_t)t.ya * G.nz + t.z || t.ya < 0 || t.ya >= G.ny ||
+                        t.z < 0 || t.z >= G.nz;
+  const bool direct_b = t.col_b != (size_t)t.yb * G.nz + t.z || t.yb < 0 || t.yb >= G.ny ||
+                        t.z < 0 || t.z >= G.nz;
+  const int L = t.x_end - t.x0 + 1;  // planes consumed: x0-1 .. x_end (relative 0..L)
+  bool bad = false;
+  int issued_hi = -1, read_lo = 0;    // thread 0's view of the copies in flight
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int r) {  // plane x0-1+r into stage r % kStages (thread 0)
+    const int s = r % kStages;
+    issued_hi = r;
+    mbar_expect_tx(&bars[s], STAGE_BYTES);
+    tma_load_plane(stages + s * SF, tmap, &bars[s], zb, y0 - 1,
+                   src_index(t.x0 - 1 + r, G.nx, open));
+  };
+  if (threadIdx.x == 0) {
+    for (int r = 0; r < kStages && r <= L; ++r) issue(r);
+  }
+  auto read = [&](int r, V2 v[5]) {
+    const int s = r % kStages;
+    read_lo = r;
+    if (!mbar_wait_bounded(&bars[s], (unsigned)((r / kStages) & 1), kTmaWaitNs)) bad = true;
+    const float* st = stages + s * SF;
+    const float* pa_ = st + (2 * w) * kBoxZ + scol;
+    const float* pb_ = pa_ + kBoxZ;
+    const float* g = src + (size_t)src_index(t.x0 - 1 + r, G.nx, open) * o.plane;
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
-      fzh[i].x = __shfl_down_sync(0xffffffffu, fzl[i].x, 1);
-      fzh[i].y = __shfl_down_sync(0xffffffffu, fzl[i].y, 1);
+      v[i].x = direct_a ? __ldg(g + i * o.vstride + t.col_a) : pa_[i * ROWS * kBoxZ];
+      v[i].y = direct_b ? __ldg(g + i * o.vstride + t.col_b) : pb_[i * ROWS * kBoxZ];
     }
-    V2 s3[5], wo[5];
-    P::update(cz, fzl, fzh, s3, K);
-    const V2 sp = P::finish(s3, wo, K);
-    float* q = dst + (size_t)x * plane;
-    if (store_a) {
-#pragma unroll
-      for (int i = 0; i < 5; ++i) q[i * vstride + dcol_a] = wo[i].x;
-      wmax = speed_max(wmax, sp.x);
-    }
-    if (store_b) {
-#pragma unroll
-      for (int i = 0; i < 5; ++i) q[i * vstride + dcol_b] = wo[i].y;
-      wmax = speed_max(wmax, sp.y);
-    }
-#pragma unroll
-    for (int i = 0; i < 5; ++i) fm[i] = fp[i];
-    cur = nxt;
   };
 
-  // Two planes per trip so the two prefetch buffers alternate without moves.
-  for (int x = x0; x < x_end; x += 2) {
-    plane_step(x, pb);
-    if (x + 1 < x_end) plane_step(x + 1, pa);
+  Cell2 cur;
+  V2 fm[5];
+  {
+    V2 w0[5], w1[5], s[5];
+    read(0, w0);
+    read(1, w1);
+    P::to_state(w0, s, K);
+    P::template derive<1>(s, cur, K);
+    Cell2 nx_;
+    P::to_state(w1, s, K);
+    P::template derive<1>(s, nx_, K);
+    P::hll(cur, nx_, fm);  // flux at face x0 - 1/2
+    cur = nx_;
   }
-  return wmax;
+  if (__syncthreads_or(bad)) {
+    *timed_out = true;
+  } else {
+    if (threadIdx.x == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      for (int r = kStages; r < kStages + 2 && r <= L; ++r) issue(r);
+    }
+    for (int x = t.x0; x < t.x_end; ++x) {
+      const int r = x - t.x0 + 2;  // plane x+1
+      V2 pf[5];
+      read(r, pf);
+      const bool stop = plane_update<P, NWP>(
+          x, pf, cur, fm, K, sm, o, []() {},
+          [&]() {
+            if (__syncthreads_or(bad)) return true;
+            if (threadIdx.x == 0 && r + kStages <= L) {
+              asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+              issue(r + kStages);
+            }
+            return false;
+          });
+      if (stop) {
+        *timed_out = true;
+        break;
+      }
+    }
+  }
+  if (*timed_out && threadIdx.x == 0) {
+    // let the copies this CTA issued land before its shared memory is released
+    for (int r = read_lo; r <= issued_hi; ++r)
+      mbar_wait_bounded(&bars[r % kStages], (unsigned)((r / kStages) & 1), kTmaWaitNs);
+  }
+  return o.wmax;
 }
 
 }  // namespace tf

@@ -1,5 +1,6 @@
 // Single-instance kernels and their C ABI: conversions, the CFL dt, the
 // fused step, the per-axis sweep and the run-to-time loop.
+#include <cuda.h>  // CUtensorMap and its enums (the encoder is fetched at run time)
 #include <math.h>
 #include <string.h>
 
@@ -194,6 +195,100 @@ __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_ker
   }
 }
 
+// The fused step with TMA-staged planes (fused_tile_tma).  The three tensor
+// maps describe src0, buf[0] and buf[1]; the loop form picks the one of the
+// current source like fused_step_kernel picks the pointer.
+template <class P, int NWP>
+__global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP))
+    fused_step_tma_kernel(FusedArgs a, const __grid_constant__ CUtensorMap tm_src0,
+                          const __grid_constant__ CUtensorMap tm_b0,
+                          const __grid_constant__ CUtensorMap tm_b1) {
+  __shared__ FusedSmem<NWP> sm;
+  __shared__ __align__(8) unsigned long long bars[kStages];
+  extern __shared__ unsigned char dyn_smem[];
+  float* stages = reinterpret_cast<float*>(
+      (reinterpret_cast<uintptr_t>(dyn_smem) + 127) & ~static_cast<uintptr_t>(127));
+  const float* src;
+  float* dst;
+  const CUtensorMap* tm;
+  float dt;
+  if (a.loop) {
+    if (!ld_volatile(&a.ctl->active)) return;
+    int iter = ld_volatile(&a.ctl->iter);
+    src = iter == 0 ? a.src0 : ((iter & 1) ? a.buf[1] : a.buf[0]);
+    tm = iter == 0 ? &tm_src0 : ((iter & 1) ? &tm_b1 : &tm_b0);
+    dst = (iter & 1) ? a.buf[0] : a.buf[1];
+    dt = a.fixed_dt > 0.f ? a.fixed_dt : ld_volatile(&a.ctl->dt);
+  } else {
+    src = a.src0;
+    tm = &tm_src0;
+    dst = a.buf[1];
+    dt = a.dt_dev ? *a.dt_dev : a.dt_host;
+  }
+  StepConsts<float> K;
+  K.g = a.gamma;
+  K.gm1 = a.gm1;
+  K.igm1 = a.igm1;
+  K.inv_dx = a.inv_dx;
+  K.dt = dt;
+  K.k = dt * a.inv_dx;
+  bool timed_out = false;
+  float m = fused_tile_tma<P, NWP>(src, dst, tm, a.geo, blockIdx.x, blockIdx.y, blockIdx.z, K,
+                                   sm, stages, bars, &timed_out);
+  if (a.ctl) {
+    float bm = block_max(m, sm.red);
+    if (threadIdx.x == 0) {
+      if (timed_out) atomicExch(&a.ctl->status, TF_ERR_TIMEOUT);
+      ctl_finish_cta(a.ctl, bm, gridDim.x * gridDim.y * gridDim.z, dt, a.loop != 0);
+    }
+  }
+}
+
+// cuTensorMapEncodeTiled, fetched from the driver through the runtime so
+// that the library does not link libcuda.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, []() {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// A [5][nx][ny][nz] float state as a 4D tensor (z, y, x, var) with the tile
+// box (kBoxZ, rows, 1, 5); false if the encoder rejects it.
+static bool make_state_tmap(CUtensorMap* m, const float* base, int nx, int ny, int nz, int rows) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  cuuint64_t dims[4] = {(cuuint64_t)nz, (cuuint64_t)ny, (cuuint64_t)nx, 5};
+  cuuint64_t strides[3] = {(cuuint64_t)nz * 4, (cuuint64_t)ny * nz * 4,
+                           (cuuint64_t)nx * ny * nz * 4};
+  cuuint32_t box[4] = {(cuuint32_t)kBoxZ, (cuuint32_t)rows, 1, 5};
+  cuuint32_t es[4] = {1, 1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides, box,
+            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+static bool tma_usable(const FusedArgs& a, int rows) {
+  if (rows != 8 && rows != 16 && rows != 32) return false;
+  if (a.geo.nz % 4 != 0) return false;  // tensor strides must be multiples of 16 bytes
+  const float* ptrs[3] = {a.src0, a.buf[0], a.buf[1]};
+  for (const float* p : ptrs)
+    if (p && (reinterpret_cast<uintptr_t>(p) & 15)) return false;
+  return encode_tiled() != nullptr;
+}
+
 static int check_dims(int nx, int ny, int nz, unsigned flags) {
   if (nx < 1 || ny < 1 || nz < 1)
     return set_error(TF_ERR_ARG, "grid dims must be >= 1 (got %d,%d,%d)", nx, ny, nz);
@@ -234,23 +329,56 @@ static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int
   return g;
 }
 
-static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx) {
+static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx, int* loader) {
   *rows = 16;  // two CTAs per SM interleave their barrier phases (measured best at 512^3)
   *lx = 0;
+  *loader = 0;
   if (tile) {
     if (!valid_tile_rows(tile->rows))
       return set_error(TF_ERR_ARG, "tile rows must be 8, 16, 32 or 34 (got %d)", tile->rows);
     *rows = tile->rows;
     *lx = tile->lx;
     if (*lx < 0) return set_error(TF_ERR_ARG, "tile lx must be >= 0");
+    if (tile->loader < 0 || tile->loader > 2)
+      return set_error(TF_ERR_ARG, "tile loader must be 0 (auto), 1 (loads) or 2 (TMA)");
+    *loader = tile->loader;
   }
   return TF_OK;
 }
 
-static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s) {
+template <int NWP>
+static int launch_tma(const FusedArgs& a, dim3 grid, const CUtensorMap* tm, bool exact,
+                      cudaStream_t s) {
+  if constexpr (NWP == 17) {
+    return set_error(TF_ERR_UNSUPPORTED, "TMA planes need 8, 16 or 32 tile rows");
+  } else {
+    const size_t smem = tma_smem_bytes(NWP) + 128;
+    auto k = exact ? fused_step_tma_kernel<ExactPair, NWP> : fused_step_tma_kernel<FastPair, NWP>;
+    TF_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem),
+                      "cudaFuncSetAttribute"));
+    k<<<grid, NWP * 32, smem, s>>>(a, tm[0], tm[1], tm[2]);
+    return TF_OK;
+  }
+}
+
+// Launches one fused step.  loader: 0 auto (TMA when usable), 1 per-thread
+// loads, 2 TMA (falls back to loads when not usable).
+static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s, int loader = 1) {
   if (a.geo.tiles_y > 65535 || a.geo.tiles_x > 65535)
     return set_error(TF_ERR_ARG, "grid too large for the tile grid");
   dim3 grid(a.geo.tiles_z, a.geo.tiles_y, a.geo.tiles_x);
+  if (loader != 1 && tma_usable(a, rows)) {
+    CUtensorMap tm[3];
+    const float* bases[3] = {a.src0, a.buf[0] ? a.buf[0] : a.src0, a.buf[1]};
+    bool ok = true;
+    for (int i = 0; i < 3 && ok; ++i)
+      ok = make_state_tmap(&tm[i], bases[i], a.geo.nx, a.geo.ny, a.geo.nz, rows);
+    if (ok) {
+      TF_DISPATCH_ROWS(rows, NWP, TF_TRY((launch_tma<NWP>(a, grid, tm, exact, s))));
+      return launch_check("fused_step_tma_kernel");
+    }
+  }
   TF_DISPATCH_ROWS(rows, NWP, {
     if (exact) fused_step_kernel<ExactPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
     else fused_step_kernel<FastPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
@@ -394,15 +522,15 @@ int tf_evolve_state(const float* W_in, float* W_out, int nx, int ny, int nz, flo
   TF_TRY(check_dims(nx, ny, nz, flags));
   TF_TRY(check_scalars(dx, gamma));
   if (!dt_dev && !isfinite(dt_host)) return set_error(TF_ERR_ARG, "dt must be finite");
-  int rows, lx;
-  TF_TRY(resolve_tile(tile, &rows, &lx));
+  int rows, lx, loader;
+  TF_TRY(resolve_tile(tile, &rows, &lx, &loader));
   FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
   FusedArgs a = make_fused_args(W_in, nullptr, W_out, geo, dx, gamma);
   a.dt_host = dt_host;
   a.dt_dev = dt_dev;
   a.loop = 0;
   a.ctl = nullptr;
-  return launch_fused(a, rows, (flags & TF_FLAG_EXACT) != 0, (cudaStream_t)stream);
+  return launch_fused(a, rows, (flags & TF_FLAG_EXACT) != 0, (cudaStream_t)stream, loader);
 }
 
 int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ctl, int nx, int ny,
@@ -419,8 +547,8 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
   if (!(fixed_dt >= 0.f) || !isfinite(fixed_dt)) return set_error(TF_ERR_ARG, "fixed_dt must be >= 0");
   if (max_steps < 0 && !isfinite(t_final))
     return set_error(TF_ERR_ARG, "an unbounded loop needs a finite t_final or max_steps >= 0");
-  int rows, lx;
-  TF_TRY(resolve_tile(tile, &rows, &lx));
+  int rows, lx, loader;
+  TF_TRY(resolve_tile(tile, &rows, &lx, &loader));
   cudaStream_t s = (cudaStream_t)stream;
   const long long n = (long long)nx * ny * nz;
   const bool exact = (flags & TF_FLAG_EXACT) != 0;
@@ -445,7 +573,7 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
 
   if (max_steps >= 0) {
     // step count known: enqueue exactly that many predicated steps
-    for (int i = 0; i < max_steps; ++i) TF_TRY(launch_fused(a, rows, exact, s));
+    for (int i = 0; i < max_steps; ++i) TF_TRY(launch_fused(a, rows, exact, s, loader));
   } else {
     // run to t_final: chunks of predicated steps, one host check per chunk
     static thread_local tf_ctl* pinned = nullptr;
@@ -454,7 +582,7 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
     long long launched = 0;
     float t_prev = -1.f;
     for (;;) {
-      for (int i = 0; i < chunk; ++i) TF_TRY(launch_fused(a, rows, exact, s));
+      for (int i = 0; i < chunk; ++i) TF_TRY(launch_fused(a, rows, exact, s, loader));
       launched += chunk;
       TF_TRY(cuda_check(cudaMemcpyAsync(pinned, ctl, sizeof(tf_ctl), cudaMemcpyDeviceToHost, s),
                         "cudaMemcpyAsync(ctl)"));
