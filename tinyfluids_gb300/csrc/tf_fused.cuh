@@ -396,6 +396,9 @@ __device__ __forceinline__ float fused_tile_tma(const float* __restrict__ src,
   if (threadIdx.x == 0) {
     for (int r = 0; r < kStages && r <= L; ++r) issue(r);
   }
+  // warps with no wrapped or clamped cell (every warp of an interior tile)
+  // read shared memory only
+  const bool warp_direct = __any_sync(0xffffffffu, direct_a || direct_b);
   auto read = [&](int r, V2 v[5]) {
     const int s = r % kStages;
     read_lo = r;
@@ -403,11 +406,19 @@ __device__ __forceinline__ float fused_tile_tma(const float* __restrict__ src,
     const float* st = stages + s * SF;
     const float* pa_ = st + (2 * w) * kBoxZ + scol;
     const float* pb_ = pa_ + kBoxZ;
-    const float* g = src + (size_t)src_index(t.x0 - 1 + r, G.nx, open) * o.plane;
+    if (!warp_direct) {
 #pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      v[i].x = direct_a ? __ldg(g + i * o.vstride + t.col_a) : pa_[i * ROWS * kBoxZ];
-      v[i].y = direct_b ? __ldg(g + i * o.vstride + t.col_b) : pb_[i * ROWS * kBoxZ];
+      for (int i = 0; i < 5; ++i) {
+        v[i].x = pa_[i * ROWS * kBoxZ];
+        v[i].y = pb_[i * ROWS * kBoxZ];
+      }
+    } else {
+      const float* g = src + (size_t)src_index(t.x0 - 1 + r, G.nx, open) * o.plane;
+#pragma unroll
+      for (int i = 0; i < 5; ++i) {
+        v[i].x = direct_a ? __ldg(g + i * o.vstride + t.col_a) : pa_[i * ROWS * kBoxZ];
+        v[i].y = direct_b ? __ldg(g + i * o.vstride + t.col_b) : pb_[i * ROWS * kBoxZ];
+      }
     }
   };
 

@@ -76,13 +76,21 @@ class _Active:
 
 
 class Server:
-    """Admits requests by free HBM budget and advances all admitted ones together."""
+    """Admits requests by free HBM budget and advances all admitted ones together.
 
-    def __init__(self, hbm_budget=120e9, device=None, tick_steps=16, rows=16,
-                 cfl=0.4, keep_states=False, max_active=4096):
+    A tick advances every active request by min(tick_steps, remaining) steps
+    in one persistent batch launch.  tick_steps is odd: a request's two
+    buffers alternate as input and output, and with the input doubling as
+    the work buffer an odd step count ends in the output buffer (no copy).
+    Batch plans are cached by the active set's buffers and step counts, which
+    recur every other tick while the set is stable, and at most two ticks are
+    in flight on the GPU."""
+
+    def __init__(self, hbm_budget=120e9, device=None, tick_steps=15, rows=16,
+                 cfl=0.4, keep_states=False, max_active=4096, plan_cache=4):
         self.device = torch.device(device if device is not None else "cuda")
         self.budget = int(hbm_budget)
-        self.tick_steps = int(tick_steps)
+        self.tick_steps = int(tick_steps) | 1
         self.rows = rows
         self.cfl = cfl
         self.keep_states = keep_states
@@ -92,6 +100,9 @@ class Server:
         self.done: list[Request] = []
         self.used = 0
         self.ticks = 0
+        self._plans: dict = {}
+        self._plan_cache = int(plan_cache)
+        self._inflight: deque = deque()
 
     # -- admission ----------------------------------------------------------
     def submit(self, req: Request):
@@ -114,36 +125,53 @@ class Server:
             req.admitted = now
 
     # -- one tick -----------------------------------------------------------
+    def _plan(self):
+        key = tuple((a.cur.data_ptr(), a.other.data_ptr(), min(self.tick_steps, a.remaining))
+                    for a in self.active)
+        b = self._plans.pop(key, None)
+        if b is None:
+            specs = [InstanceSpec(a.cur, a.dx, a.req.gamma,
+                                  num_steps=min(self.tick_steps, a.remaining), C_CFL=self.cfl,
+                                  out=a.other, consume_input=True) for a in self.active]
+            b = Batch(specs, rows=self.rows)
+            while len(self._plans) >= self._plan_cache:
+                old = self._plans.pop(next(iter(self._plans)))
+                old.close()
+        self._plans[key] = b  # most recently used last
+        return b
+
     def _tick(self):
-        specs = []
-        for a in self.active:
-            k = min(self.tick_steps, a.remaining)
-            specs.append(InstanceSpec(a.cur, a.dx, a.req.gamma, num_steps=k, C_CFL=self.cfl,
-                                      out=a.other, consume_input=True))
-        b = Batch(specs, rows=self.rows)
+        b = self._plan()
         b.run()
-        torch.cuda.current_stream(self.device).synchronize()
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self.device))
+        self._inflight.append(ev)
+        while len(self._inflight) > 2:
+            self._inflight.popleft().synchronize()
         self.ticks += 1
-        for a, sp in zip(self.active, specs):
+        for a, sp in zip(self.active, b.specs):
             a.cur, a.other = a.other, a.cur  # the result is in `out`
             a.remaining -= sp.num_steps
-        b.close()
 
-    def _retire(self, now):
-        keep = []
-        for a in self.active:
-            if a.remaining > 0:
-                keep.append(a)
-                continue
-            rho = a.cur[0]
-            a.req.result = {"mass": float(rho.double().sum()) * a.dx ** 3,
-                            "rho_max": float(rho.max())}
+    def _retire(self):
+        finishing = [a for a in self.active if a.remaining <= 0]
+        if not finishing:
+            return
+        self.active = [a for a in self.active if a.remaining > 0]
+        masses = [a.cur[0].double().sum() for a in finishing]
+        rmax = [a.cur[0].max() for a in finishing]
+        torch.cuda.current_stream(self.device).synchronize()
+        self._inflight.clear()
+        now = self._now()
+        for a, m, r in zip(finishing, masses, rmax):
+            a.req.result = {"mass": float(m) * a.dx ** 3, "rho_max": float(r)}
             if self.keep_states:
                 a.req.result["state"] = a.cur
             a.req.finished = now
             self.used -= request_bytes(a.req.n)
             self.done.append(a.req)
-        self.active = keep
+        # plans that refer to retired buffers can never recur
+        self._plans.clear()
 
     # -- event loop ---------------------------------------------------------
     def serve(self, requests, clock=None, idle_sleep=2e-4):
@@ -151,16 +179,22 @@ class Server:
         for r in sorted(requests, key=lambda r: r.arrival):
             self.submit(r)
         t0 = time.perf_counter()
-        now = (lambda: time.perf_counter() - t0) if clock is None else clock
+        self._now = (lambda: time.perf_counter() - t0) if clock is None else clock
         while self.queue or self.active:
-            self._admit(now())
+            n_before = len(self.active)
+            self._admit(self._now())
+            if len(self.active) != n_before:
+                self._plans.clear()
             if not self.active:
                 nxt = self.queue[0].arrival
-                while now() < nxt:
-                    time.sleep(min(idle_sleep, max(0.0, nxt - now())))
+                while self._now() < nxt:
+                    time.sleep(min(idle_sleep, max(0.0, nxt - self._now())))
                 continue
             self._tick()
-            self._retire(now())
+            self._retire()
+        for b in self._plans.values():
+            b.close()
+        self._plans.clear()
         return self.done
 
 
