@@ -73,7 +73,8 @@ typedef struct tf_tile_config {
   int rows;    /* grid rows per tile incl. the 1-cell ring: 8, 16, 32 or 34 (rows/2 warps) */
   int lx;      /* x planes per CTA (>= 1; 0 = heuristic) */
   int loader;  /* 0 = auto, 1 = per-thread loads, 2 = TMA-staged planes (needs nz % 4 == 0,
-                  16-byte aligned states and rows 8, 16 or 32; falls back otherwise) */
+                  16-byte aligned states and rows 8, 16 or 32; falls back otherwise),
+                  3 = per-thread loads with the software-pipelined plane loop */
 } tf_tile_config;
 
 int tf_abi_version(void);

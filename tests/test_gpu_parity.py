@@ -209,7 +209,7 @@ def test_time_integration_zero_and_negative_t_final(tg):
 
 
 @pytest.mark.parametrize("shape", [(16, 16, 16), (40, 31, 64), (7, 9, 4), (5, 45, 8),
-                                   (33, 17, 60), (2, 2, 12), (130, 3, 4)])
+                                   (33, 17, 60), (2, 2, 12), (130, 3, 4), (1, 5, 8), (3, 3, 33)])
 @pytest.mark.parametrize("hb", [False, True])
 @pytest.mark.parametrize("exact", [False, True])
 def test_tma_and_load_planes_agree_bitwise(tg, shape, hb, exact):
@@ -222,7 +222,10 @@ def test_tma_and_load_planes_agree_bitwise(tg, shape, hb, exact):
     for rows, lx in ((8, 3), (16, 0), (32, 5)):
         a = tg._evolve_state(Wd, 0.05, float(dt), GAMMA, hb, exact=exact, tile=(rows, lx, "ldg"))
         b = tg._evolve_state(Wd, 0.05, float(dt), GAMMA, hb, exact=exact, tile=(rows, lx, "tma"))
+        c = tg._evolve_state(Wd, 0.05, float(dt), GAMMA, hb, exact=exact,
+                             tile=(rows, lx, "pipelined"))
         assert torch.equal(a, b), (rows, lx)
+        assert torch.equal(a, c), (rows, lx)
     if exact:
         assert np.array_equal(host(b), F._evolve_state(W, 0.05, dt, GAMMA, hb))
 
@@ -231,4 +234,5 @@ def test_tma_loop_matches_load_loop(tg):
     W, dx = tg.shear_layer(64, seed=2)
     a = tg.run_steps(W, dx, GAMMA, 9, tile=(16, 16, "ldg"))
     b = tg.run_steps(W, dx, GAMMA, 9, tile=(16, 16, "tma"))
-    assert torch.equal(a, b)
+    c = tg.run_steps(W, dx, GAMMA, 9, tile=(16, 16, "pipelined"))
+    assert torch.equal(a, b) and torch.equal(a, c)

@@ -279,6 +279,157 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
 }
 
 // ---------------------------------------------------------------------------
+// Software-pipelined plane loop
+// ---------------------------------------------------------------------------
+// The same arithmetic as fused_tile, with the loop rotated so that the z
+// sweep of plane x and the x sweep of plane x+1 -- two independent
+// dependency chains -- sit in one barrier-free block the compiler can
+// interleave.  Per trip: y sweep of x (two barriers), then {z sweep and store
+// of x} with {x sweep of x+1}.
+template <class P, int NWP, bool COHERENT = false>
+__device__ __forceinline__ float fused_tile_pipelined(const float* __restrict__ src,
+                                                      float* __restrict__ dst,
+                                                      const FusedGeom& G, int tz, int ty,
+                                                      int tx, const StepConsts<float>& K,
+                                                      FusedSmem<NWP>& sm) {
+  TileOut o;
+  const TileCols t = tile_cols<NWP>(G, tz, ty, tx, src, dst, o);
+  const bool open = G.open_bc != 0;
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  auto load = [&](int x, V2 v[5]) {
+    const float* p = src + (size_t)src_index(x, G.nx, open) * o.plane;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      const float* q = p + i * o.vstride;
+      v[i].x = COHERENT ? __ldcg(q + t.col_a) : __ldg(q + t.col_a);
+      v[i].y = COHERENT ? __ldcg(q + t.col_b) : __ldg(q + t.col_b);
+    }
+  };
+  // x sweep of one plane: cur = plane x, pf = plane x+1 -> s1 (plane x), and
+  // the carry moves to plane x+1
+  Cell2 cur;
+  V2 fm[5];
+  auto x_sweep = [&](const V2 pf[5], V2 s1[5]) {
+    V2 s[5];
+    Cell2 nxt;
+    P::to_state(pf, s, K);
+    P::template derive<1>(s, nxt, K);
+    V2 fp[5];
+    P::hll(cur, nxt, fp);
+    P::update(cur, fm, fp, s1, K);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) fm[i] = fp[i];
+    cur = nxt;
+  };
+  V2 pa[5], pb[5], s1[5];
+  {
+    V2 w0[5], w1[5], s[5];
+    load(t.x0 - 1, w0);
+    load(t.x0, w1);
+    load(t.x0 + 1, pa);
+    load(t.x0 + 2 <= t.x_end ? t.x0 + 2 : t.x_end, pb);
+    P::to_state(w0, s, K);
+    P::template derive<1>(s, cur, K);
+    Cell2 nx_;
+    P::to_state(w1, s, K);
+    P::template derive<1>(s, nx_, K);
+    P::hll(cur, nx_, fm);  // flux at face x0 - 1/2
+    cur = nx_;
+    x_sweep(pa, s1);  // plane x0
+    if (t.x0 + 3 <= t.x_end) load(t.x0 + 3, pa);
+  }
+  // y and z sweeps of plane x from s1; x sweep of plane x+1 from pf (plane
+  // x+2) into s1; pf then receives plane x+4
+  auto trip = [&](int x, V2 pf[5]) {
+    Cell2 cy;
+    P::template derive<2>(s1, cy, K);
+    sm.cy[0][w][lane] = make_float4(cy.U[0].y, cy.U[1].y, cy.U[2].y, cy.U[3].y);
+    sm.cy[1][w][lane] = make_float4(cy.U[4].y, cy.F[0].y, cy.F[1].y, cy.F[2].y);
+    sm.cy[2][w][lane] = make_float4(cy.F[3].y, cy.F[4].y, cy.u.y, cy.c.y);
+    __syncthreads();
+    Cell2 L;
+    {
+      float4 a, b, d;
+      if (w >= 1) {
+        a = sm.cy[0][w - 1][lane];
+        b = sm.cy[1][w - 1][lane];
+        d = sm.cy[2][w - 1][lane];
+      } else {
+        a = make_float4(cy.U[0].x, cy.U[1].x, cy.U[2].x, cy.U[3].x);
+        b = make_float4(cy.U[4].x, cy.F[0].x, cy.F[1].x, cy.F[2].x);
+        d = make_float4(cy.F[3].x, cy.F[4].x, cy.u.x, cy.c.x);
+      }
+      L.U[0] = v2(a.x, cy.U[0].x); L.U[1] = v2(a.y, cy.U[1].x);
+      L.U[2] = v2(a.z, cy.U[2].x); L.U[3] = v2(a.w, cy.U[3].x);
+      L.U[4] = v2(b.x, cy.U[4].x); L.F[0] = v2(b.y, cy.F[0].x);
+      L.F[1] = v2(b.z, cy.F[1].x); L.F[2] = v2(b.w, cy.F[2].x);
+      L.F[3] = v2(d.x, cy.F[3].x); L.F[4] = v2(d.y, cy.F[4].x);
+      L.u = v2(d.z, cy.u.x);       L.c = v2(d.w, cy.c.x);
+    }
+    V2 fy[5];
+    P::hll(L, cy, fy);
+    sm.fy4[w][lane] = make_float4(fy[0].x, fy[1].x, fy[2].x, fy[3].x);
+    sm.fy1[w][lane] = fy[4].x;
+    __syncthreads();
+    V2 fyh[5];
+    {
+      float4 f4;
+      float f1;
+      if (w <= NWP - 2) {
+        f4 = sm.fy4[w + 1][lane];
+        f1 = sm.fy1[w + 1][lane];
+      } else {
+        f4 = make_float4(fy[0].x, fy[1].x, fy[2].x, fy[3].x);
+        f1 = fy[4].x;
+      }
+      fyh[0] = v2(fy[0].y, f4.x);
+      fyh[1] = v2(fy[1].y, f4.y);
+      fyh[2] = v2(fy[2].y, f4.z);
+      fyh[3] = v2(fy[3].y, f4.w);
+      fyh[4] = v2(fy[4].y, f1);
+    }
+    V2 s2[5];
+    P::update(cy, fy, fyh, s2, K);
+    // ---- barrier-free block: z sweep of x and x sweep of x+1 ----
+    if (x + 1 < t.x_end) {
+      x_sweep(pf, s1);
+      if (x + 4 <= t.x_end) load(x + 4, pf);
+    }
+    Cell2 cz, nb;
+    P::template derive<3>(s2, cz, K);
+    shfl_up_cell2(cz, nb);
+    V2 fzl[5], fzh[5];
+    P::hll(nb, cz, fzl);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      fzh[i].x = __shfl_down_sync(0xffffffffu, fzl[i].x, 1);
+      fzh[i].y = __shfl_down_sync(0xffffffffu, fzl[i].y, 1);
+    }
+    V2 s3[5], wo[5];
+    P::update(cz, fzl, fzh, s3, K);
+    const V2 sp = P::finish(s3, wo, K);
+    float* q = o.dst + (size_t)x * o.plane;
+    if (o.store_a) {
+#pragma unroll
+      for (int i = 0; i < 5; ++i) q[i * o.vstride + o.dcol_a] = wo[i].x;
+      o.wmax = speed_max(o.wmax, sp.x);
+    }
+    if (o.store_b) {
+#pragma unroll
+      for (int i = 0; i < 5; ++i) q[i * o.vstride + o.dcol_b] = wo[i].y;
+      o.wmax = speed_max(o.wmax, sp.y);
+    }
+  };
+  // planes x+2 alternate between pb (x even offset) and pa
+  for (int x = t.x0; x < t.x_end; x += 2) {
+    trip(x, pb);
+    if (x + 1 < t.x_end) trip(x + 1, pa);
+  }
+  return o.wmax;
+}
+
+// ---------------------------------------------------------------------------
 // TMA-staged planes
 // ---------------------------------------------------------------------------
 // One elected thread copies each x plane of the tile -- all five variables,

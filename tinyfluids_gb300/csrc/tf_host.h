@@ -27,9 +27,14 @@ int sm_count();  // multiprocessors of the current device (cached per device)
 // instantiated for; the kernel uses rows/2 warps.
 inline bool valid_tile_rows(int rows) { return rows == 8 || rows == 16 || rows == 32 || rows == 34; }
 
-// CTAs per SM the fused kernels are register-bounded for: 16 warps per SM
-// for every tile height.
-__host__ __device__ constexpr int min_ctas_per_sm(int nwp) { return nwp >= 16 ? 1 : 16 / nwp; }
+// CTAs per SM the fused kernels are register-bounded for: TF_WARPS_PER_SM
+// (16 by default) warps per SM for every tile height.
+#ifndef TF_WARPS_PER_SM
+#define TF_WARPS_PER_SM 16
+#endif
+__host__ __device__ constexpr int min_ctas_per_sm(int nwp) {
+  return nwp >= TF_WARPS_PER_SM ? 1 : TF_WARPS_PER_SM / nwp;
+}
 
 #define TF_DISPATCH_ROWS(rows, NWP, ...)          \
   switch (rows) {                                 \

@@ -163,7 +163,7 @@ struct FusedArgs {
   int loop;        // 1: predicated loop step (parity buffers, dt from ctl)
 };
 
-template <class P, int NWP>
+template <class P, int NWP, bool PIPELINED = false>
 __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_kernel(FusedArgs a) {
   __shared__ FusedSmem<NWP> sm;
   const float* src;
@@ -187,7 +187,10 @@ __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_ker
   K.inv_dx = a.inv_dx;
   K.dt = dt;
   K.k = dt * a.inv_dx;
-  float m = fused_tile<P, NWP>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z, K, sm);
+  float m = PIPELINED ? fused_tile_pipelined<P, NWP>(src, dst, a.geo, blockIdx.x, blockIdx.y,
+                                                     blockIdx.z, K, sm)
+                      : fused_tile<P, NWP>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z, K,
+                                           sm);
   if (a.ctl) {
     float bm = block_max(m, sm.red);
     if (threadIdx.x == 0)
@@ -339,8 +342,9 @@ static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx, int* loa
     *rows = tile->rows;
     *lx = tile->lx;
     if (*lx < 0) return set_error(TF_ERR_ARG, "tile lx must be >= 0");
-    if (tile->loader < 0 || tile->loader > 2)
-      return set_error(TF_ERR_ARG, "tile loader must be 0 (auto), 1 (loads) or 2 (TMA)");
+    if (tile->loader < 0 || tile->loader > 3)
+      return set_error(TF_ERR_ARG,
+                       "tile loader must be 0 (auto), 1 (loads), 2 (TMA) or 3 (pipelined loads)");
     *loader = tile->loader;
   }
   return TF_OK;
@@ -380,6 +384,13 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
       TF_DISPATCH_ROWS(rows, NWP, TF_TRY((launch_tma<NWP>(a, grid, tm, exact, s))));
       return launch_check("fused_step_tma_kernel");
     }
+  }
+  if (loader == 3) {
+    TF_DISPATCH_ROWS(rows, NWP, {
+      if (exact) fused_step_kernel<ExactPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
+      else fused_step_kernel<FastPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
+    });
+    return launch_check("fused_step_kernel");
   }
   TF_DISPATCH_ROWS(rows, NWP, {
     if (exact) fused_step_kernel<ExactPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
