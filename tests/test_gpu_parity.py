@@ -216,6 +216,8 @@ def test_tma_and_load_planes_agree_bitwise(tg, shape, hb, exact):
     """TMA-staged planes (shared-memory ring) and per-thread loads feed the same
     arithmetic: identical results, for every tile height, ragged and wrapped
     edges included; the exact form also equals the oracle."""
+    if hb and min(shape) < 2:
+        pytest.skip("open boundaries need two cells per axis")
     W = random_state(shape, 41)
     dt = F._cfl_time_step(W, 0.05, GAMMA)
     Wd = dev(W)

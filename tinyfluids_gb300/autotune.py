@@ -11,9 +11,10 @@ device and keeps the fastest.  Results are cached per (GPU, grid shape,
 arithmetic) in memory and in a JSON file (``$TINYFLUIDS_GB300_TUNE_CACHE`` or
 ``~/.cache/tinyfluids_gb300/tiles.json``).
 
-Batches use ``size_class``: instances are grouped by their largest axis into
-classes, each class is tuned once on a representative cube, and every instance
-of the class uses that class's ``lx`` under the batch's common ``rows``.
+Batches (``tune_batch``) are tuned on the batch itself: every (rows, lx
+policy) candidate runs a few steps of the actual batch and the fastest wins,
+because inside a full batch the best tile differs from the best tile for a
+grid running alone.
 """
 from __future__ import annotations
 
@@ -136,29 +137,42 @@ def size_class(n: int) -> int:
     return SIZE_CLASSES[-1]
 
 
-def tune_batch(shapes, exact=False, device=None):
+def tune_batch(specs, exact=False, device=None, steps=2, candidates_rows=ROWS,
+               lx_policies=(0, 64, 32)):
     """Tile choice for a batch: one `rows` for the launch and an `lx` per
-    instance.  Each size class is tuned once on its representative cube; the
-    batch takes the rows that minimise the cell-weighted sum of per-class
-    times, and each class its best lx under those rows."""
-    classes = {}
-    for s in shapes:
-        c = size_class(max(s))
-        classes.setdefault(c, 0)
-        classes[c] += s[0] * s[1] * s[2]
-    results = {c: tune((c, c, c), exact=exact, device=device) for c in classes}
-    best_rows, best_cost = None, float("inf")
-    for rows in ROWS:
-        cost = 0.0
-        for c, cells in classes.items():
-            ts = [t for k, t in results[c]["table"].items() if int(k.split(",")[0]) == rows]
-            cost += cells / c ** 3 * min(ts)
-        if cost < best_cost:
-            best_rows, best_cost = rows, cost
-    lx_by_class = {}
-    for c in classes:
-        items = [(t, int(k.split(",")[1])) for k, t in results[c]["table"].items()
-                 if int(k.split(",")[0]) == best_rows]
-        lx_by_class[c] = min(items)[1]
-    lxs = [min(lx_by_class[size_class(max(s))], s[0]) for s in shapes]
-    return best_rows, lxs
+    instance.  Inside a batch the GPU is full, so single-grid timings are a
+    poor proxy; the candidates are timed on the batch itself (a short run of
+    `steps` steps on copies of its states).  lx policy 0 means the whole x
+    extent per CTA, otherwise min(nx, policy).  Cached per list of shapes."""
+    from dataclasses import replace
+    from .batching import Batch
+    shapes = tuple(tuple(sp.state.shape[1:]) for sp in specs)
+    dev = torch.device(device if device is not None else specs[0].state.device)
+    key = ("batch", torch.cuda.get_device_name(dev), shapes, bool(exact))
+    with _LOCK:
+        if key in _MEM:
+            return _MEM[key]
+    best = None
+    for rows in candidates_rows:
+        for pol in lx_policies:
+            lxs = [s[0] if pol == 0 else min(s[0], pol) for s in shapes]
+            trial = [replace(sp, num_steps=steps, t_final=float("inf"), fixed_dt=None,
+                             lx=lx, out=None, consume_input=False)
+                     for sp, lx in zip(specs, lxs)]
+            b = Batch(trial, rows=rows, exact=exact, autotune=False)
+            b.run()
+            st = torch.cuda.current_stream(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            b.run()
+            e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            b.close()
+            del b
+            if best is None or ms < best[0]:
+                best = (ms, rows, lxs)
+    res = (best[1], best[2])
+    with _LOCK:
+        _MEM[key] = res
+    return res

@@ -68,8 +68,7 @@ class Batch:
         self.steps = int(steps)
         if autotune:
             from . import autotune as _at
-            rows, lxs = _at.tune_batch([tuple(sp.state.shape[1:]) for sp in self.specs],
-                                       exact=self.exact, device=dev)
+            rows, lxs = _at.tune_batch(self.specs, exact=self.exact, device=dev)
             self.specs = [sp if sp.lx else _replace(sp, lx=lx) for sp, lx in zip(self.specs, lxs)]
         self.rows = int(rows)
         with torch.cuda.device(dev):
