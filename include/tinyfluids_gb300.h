@@ -70,11 +70,10 @@ typedef struct tf_ctl {
 /* Tile shape of the fused step kernel; NULL = built-in heuristic (16 rows,
  * lx for about eight waves of resident CTAs). */
 typedef struct tf_tile_config {
-  int rows;    /* grid rows per tile incl. the 1-cell ring: 8, 16, 32 or 34 (rows/2 warps) */
+  int rows;    /* grid rows per tile incl. the 1-cell ring: 8, 16 or 32 (rows/2 warps) */
   int lx;      /* x planes per CTA (>= 1; 0 = heuristic) */
-  int loader;  /* 0 = auto, 1 = per-thread loads, 2 = TMA-staged planes (needs nz % 4 == 0,
-                  16-byte aligned states and rows 8, 16 or 32; falls back otherwise),
-                  3 = per-thread loads with the software-pipelined plane loop */
+  int loader;  /* 0 = auto (per-thread loads), 1 = per-thread loads, 2 = TMA-staged planes
+                  (needs nz % 4 == 0 and 16-byte aligned states; falls back otherwise) */
 } tf_tile_config;
 
 int tf_abi_version(void);
@@ -213,7 +212,7 @@ typedef struct tf_instance {
 } tf_instance;
 
 typedef struct tf_batch_config {
-  int rows;          /* grid rows per tile: 8, 16, 32 or 34 (see tf_tile_config) */
+  int rows;          /* grid rows per tile: 8, 16 or 32 (see tf_tile_config) */
   int exact;         /* nonzero: reference op order */
   int persistent;    /* nonzero: one persistent launch for all steps; else one launch per step */
   int ctas_per_sm;   /* persistent grid = ctas_per_sm * SMs (0 = occupancy limit) */

@@ -69,7 +69,7 @@ def test_host_side_argument_checks(lib):
     with pytest.raises(_lib.TinyfluidsError):  # gamma == 1
         _lib.call("tf_evolve_state", fake, other, 4, 4, 4, 0.1, 0.01, None, 1.0, 0, None, None)
     with pytest.raises(_lib.TinyfluidsError):  # bad tile rows
-        tc = _lib.TileConfig(12, 4)  # not one of 8, 16, 32, 34
+        tc = _lib.TileConfig(34, 4, 0)  # not one of 8, 16, 32
         _lib.call("tf_evolve_state", fake, other, 4, 4, 4, 0.1, 0.01, None, 5 / 3, 0,
                   ctypes.byref(tc), None)
     with pytest.raises(_lib.TinyfluidsError):  # unbounded loop

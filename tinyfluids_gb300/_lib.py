@@ -24,7 +24,7 @@ c_char_p = ctypes.c_char_p
 
 
 class TileConfig(ctypes.Structure):
-    """tf_tile_config: tile rows (8, 16, 32, 34), x planes per CTA, plane loader
+    """tf_tile_config: tile rows (8, 16, 32), x planes per CTA, plane loader
     (0 auto, 1 per-thread loads, 2 TMA-staged)."""
     _fields_ = [("rows", c_int), ("lx", c_int), ("loader", c_int)]
 

@@ -1,7 +1,7 @@
 """Tile-shape autotuner for the fused step kernel.
 
 The fused kernel's tile has two free parameters (``tf_tile_config``): the tile
-height ``rows`` (8, 16, 32 or 34 grid rows incl. the one-cell ring; the kernel
+height ``rows`` (8, 16 or 32 grid rows incl. the one-cell ring; the kernel
 runs rows/2 warps) and ``lx``, the number of x planes one CTA marches through.
 Taller tiles waste fewer halo rows; shorter ones let two or more CTAs share an
 SM and interleave their barrier phases; ``lx`` trades per-chunk warm-up work

@@ -79,6 +79,23 @@ struct TileOut {
   float wmax;
 };
 
+// Element offsets are 32-bit (IDX32) when the whole state has fewer than
+// 2^31 floats, which halves the address arithmetic of every access.
+template <bool IDX32>
+__device__ __forceinline__ void store5(const TileOut& o, int x, size_t dcol, const V2 wo[5],
+                                       bool hi) {
+  if (IDX32) {
+    const unsigned base = (unsigned)x * (unsigned)o.plane + (unsigned)dcol;
+    const unsigned vs = (unsigned)o.vstride;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) o.dst[base + (unsigned)i * vs] = hi ? wo[i].y : wo[i].x;
+  } else {
+    float* q = o.dst + (size_t)x * o.plane + dcol;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) q[i * o.vstride] = hi ? wo[i].y : wo[i].x;
+  }
+}
+
 // One plane of the fused step for the thread's pair of cells: the x sweep
 // from registers (cur = plane x, pf = plane x+1, fm = flux at x-1/2), then
 // the y and z sweeps, the store and the CFL epilogue.  `consumed()` runs as
@@ -86,18 +103,19 @@ struct TileOut {
 // `after_sync()` runs after the plane's first CTA barrier, when every thread
 // has read plane x+1 (the TMA loader refills its stage there) and returns
 // true if the CTA must stop (a bounded wait gave up).
-template <class P, int NWP, class Consumed, class AfterSync>
-__device__ __forceinline__ bool plane_update(int x, V2 pf[5], Cell2& cur, V2 fm[5],
-                                             const StepConsts<float>& K, FusedSmem<NWP>& sm,
-                                             TileOut& o, Consumed consumed, AfterSync after_sync) {
+template <class P, int NWP, bool IDX32, class Consumed, class AfterSync>
+__device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, const V2 fm[5],
+                                             Cell2& nxt, V2 fp[5], const StepConsts<float>& K,
+                                             FusedSmem<NWP>& sm, TileOut& o, Consumed consumed,
+                                             AfterSync after_sync) {
+  // cur / fm: plane x and the flux at x-1/2; nxt / fp receive plane x+1 and
+  // the flux at x+1/2 (the caller alternates two carries instead of copying)
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   V2 s[5];
-  Cell2 nxt;
   P::to_state(pf, s, K);
   P::template derive<1>(s, nxt, K);
   consumed();
-  V2 fp[5];
   P::hll(cur, nxt, fp);  // face x + 1/2
   V2 s1[5];
   P::update(cur, fm, fp, s1, K);
@@ -172,20 +190,14 @@ __device__ __forceinline__ bool plane_update(int x, V2 pf[5], Cell2& cur, V2 fm[
   V2 s3[5], wo[5];
   P::update(cz, fzl, fzh, s3, K);
   const V2 sp = P::finish(s3, wo, K);
-  float* q = o.dst + (size_t)x * o.plane;
   if (o.store_a) {
-#pragma unroll
-    for (int i = 0; i < 5; ++i) q[i * o.vstride + o.dcol_a] = wo[i].x;
+    store5<IDX32>(o, x, o.dcol_a, wo, false);
     o.wmax = speed_max(o.wmax, sp.x);
   }
   if (o.store_b) {
-#pragma unroll
-    for (int i = 0; i < 5; ++i) q[i * o.vstride + o.dcol_b] = wo[i].y;
+    store5<IDX32>(o, x, o.dcol_b, wo, true);
     o.wmax = speed_max(o.wmax, sp.y);
   }
-#pragma unroll
-  for (int i = 0; i < 5; ++i) fm[i] = fp[i];
-  cur = nxt;
   return stop;
 }
 
@@ -229,24 +241,37 @@ __device__ __forceinline__ TileCols tile_cols(const FusedGeom& G, int tz, int ty
 // L2-only loads (ld.global.cg) for kernels that read data other CTAs wrote
 // earlier in the same launch (the persistent batch kernel); otherwise loads
 // use the read-only path.
-template <class P, int NWP, bool COHERENT = false>
+template <class P, int NWP, bool COHERENT = false, bool IDX32 = false>
 __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float* __restrict__ dst,
                                             const FusedGeom& G, int tz, int ty, int tx,
                                             const StepConsts<float>& K, FusedSmem<NWP>& sm) {
   TileOut o;
   const TileCols t = tile_cols<NWP>(G, tz, ty, tx, src, dst, o);
   const bool open = G.open_bc != 0;
+  const unsigned vs32 = (unsigned)o.vstride, pl32 = (unsigned)o.plane;
+  const unsigned ca32 = (unsigned)t.col_a, cb32 = (unsigned)t.col_b;
+  auto ld = [&](const float* p) { return COHERENT ? __ldcg(p) : __ldg(p); };
   auto load = [&](int x, V2 v[5]) {
-    const float* p = src + (size_t)src_index(x, G.nx, open) * o.plane;
+    const int xs = src_index(x, G.nx, open);
+    if (IDX32) {
+      const unsigned po = (unsigned)xs * pl32;
 #pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      const float* q = p + i * o.vstride;
-      v[i].x = COHERENT ? __ldcg(q + t.col_a) : __ldg(q + t.col_a);
-      v[i].y = COHERENT ? __ldcg(q + t.col_b) : __ldg(q + t.col_b);
+      for (int i = 0; i < 5; ++i) {
+        v[i].x = ld(src + (po + ca32 + (unsigned)i * vs32));
+        v[i].y = ld(src + (po + cb32 + (unsigned)i * vs32));
+      }
+    } else {
+      const float* p = src + (size_t)xs * o.plane;
+#pragma unroll
+      for (int i = 0; i < 5; ++i) {
+        const float* q = p + i * o.vstride;
+        v[i].x = ld(q + t.col_a);
+        v[i].y = ld(q + t.col_b);
+      }
     }
   };
-  Cell2 cur;
-  V2 fm[5];
+  Cell2 c0, c1;  // carried plane quantities, alternating roles
+  V2 f0[5], f1[5];
   V2 pa[5], pb[5];
   {
     V2 w0[5], s[5];
@@ -254,177 +279,39 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
     load(t.x0, pa);
     load(t.x0 + 1, pb);
     P::to_state(w0, s, K);
-    P::template derive<1>(s, cur, K);
-    Cell2 nx_;
+    P::template derive<1>(s, c1, K);
     P::to_state(pa, s, K);
-    P::template derive<1>(s, nx_, K);
+    P::template derive<1>(s, c0, K);
     if (t.x0 + 2 <= t.x_end) load(t.x0 + 2, pa);
-    P::hll(cur, nx_, fm);  // flux at face x0 - 1/2
-    cur = nx_;
+    P::hll(c1, c0, f0);  // flux at face x0 - 1/2; c0 = plane x0
   }
   auto sync_only = []() {
     __syncthreads();
     return false;
   };
-  // Two planes per trip so the two prefetch buffers alternate without moves;
+  // Two planes per trip so the prefetch buffers alternate without moves;
   // `pf` holds plane x+1 on entry and receives plane x+3.
   for (int x = t.x0; x < t.x_end; x += 2) {
-    plane_update<P, NWP>(x, pb, cur, fm, K, sm, o,
-                         [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); }, sync_only);
-    if (x + 1 < t.x_end)
-      plane_update<P, NWP>(x + 1, pa, cur, fm, K, sm, o,
-                           [&]() { if (x + 4 <= t.x_end) load(x + 4, pa); }, sync_only);
-  }
-  return o.wmax;
-}
-
-// ---------------------------------------------------------------------------
-// Software-pipelined plane loop
-// ---------------------------------------------------------------------------
-// The same arithmetic as fused_tile, with the loop rotated so that the z
-// sweep of plane x and the x sweep of plane x+1 -- two independent
-// dependency chains -- sit in one barrier-free block the compiler can
-// interleave.  Per trip: y sweep of x (two barriers), then {z sweep and store
-// of x} with {x sweep of x+1}.
-template <class P, int NWP, bool COHERENT = false>
-__device__ __forceinline__ float fused_tile_pipelined(const float* __restrict__ src,
-                                                      float* __restrict__ dst,
-                                                      const FusedGeom& G, int tz, int ty,
-                                                      int tx, const StepConsts<float>& K,
-                                                      FusedSmem<NWP>& sm) {
-  TileOut o;
-  const TileCols t = tile_cols<NWP>(G, tz, ty, tx, src, dst, o);
-  const bool open = G.open_bc != 0;
-  const int lane = threadIdx.x & 31;
-  const int w = threadIdx.x >> 5;
-  auto load = [&](int x, V2 v[5]) {
-    const float* p = src + (size_t)src_index(x, G.nx, open) * o.plane;
+#ifndef TF_CARRY_PINGPONG  // the carry is copied back after each plane (fewer live registers)
+    plane_update<P, NWP, IDX32>(x, pb, c0, f0, c1, f1, K, sm, o,
+                                [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); }, sync_only);
+    c0 = c1;
 #pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      const float* q = p + i * o.vstride;
-      v[i].x = COHERENT ? __ldcg(q + t.col_a) : __ldg(q + t.col_a);
-      v[i].y = COHERENT ? __ldcg(q + t.col_b) : __ldg(q + t.col_b);
-    }
-  };
-  // x sweep of one plane: cur = plane x, pf = plane x+1 -> s1 (plane x), and
-  // the carry moves to plane x+1
-  Cell2 cur;
-  V2 fm[5];
-  auto x_sweep = [&](const V2 pf[5], V2 s1[5]) {
-    V2 s[5];
-    Cell2 nxt;
-    P::to_state(pf, s, K);
-    P::template derive<1>(s, nxt, K);
-    V2 fp[5];
-    P::hll(cur, nxt, fp);
-    P::update(cur, fm, fp, s1, K);
-#pragma unroll
-    for (int i = 0; i < 5; ++i) fm[i] = fp[i];
-    cur = nxt;
-  };
-  V2 pa[5], pb[5], s1[5];
-  {
-    V2 w0[5], w1[5], s[5];
-    load(t.x0 - 1, w0);
-    load(t.x0, w1);
-    load(t.x0 + 1, pa);
-    load(t.x0 + 2 <= t.x_end ? t.x0 + 2 : t.x_end, pb);
-    P::to_state(w0, s, K);
-    P::template derive<1>(s, cur, K);
-    Cell2 nx_;
-    P::to_state(w1, s, K);
-    P::template derive<1>(s, nx_, K);
-    P::hll(cur, nx_, fm);  // flux at face x0 - 1/2
-    cur = nx_;
-    x_sweep(pa, s1);  // plane x0
-    if (t.x0 + 3 <= t.x_end) load(t.x0 + 3, pa);
-  }
-  // y and z sweeps of plane x from s1; x sweep of plane x+1 from pf (plane
-  // x+2) into s1; pf then receives plane x+4
-  auto trip = [&](int x, V2 pf[5]) {
-    Cell2 cy;
-    P::template derive<2>(s1, cy, K);
-    sm.cy[0][w][lane] = make_float4(cy.U[0].y, cy.U[1].y, cy.U[2].y, cy.U[3].y);
-    sm.cy[1][w][lane] = make_float4(cy.U[4].y, cy.F[0].y, cy.F[1].y, cy.F[2].y);
-    sm.cy[2][w][lane] = make_float4(cy.F[3].y, cy.F[4].y, cy.u.y, cy.c.y);
-    __syncthreads();
-    Cell2 L;
-    {
-      float4 a, b, d;
-      if (w >= 1) {
-        a = sm.cy[0][w - 1][lane];
-        b = sm.cy[1][w - 1][lane];
-        d = sm.cy[2][w - 1][lane];
-      } else {
-        a = make_float4(cy.U[0].x, cy.U[1].x, cy.U[2].x, cy.U[3].x);
-        b = make_float4(cy.U[4].x, cy.F[0].x, cy.F[1].x, cy.F[2].x);
-        d = make_float4(cy.F[3].x, cy.F[4].x, cy.u.x, cy.c.x);
-      }
-      L.U[0] = v2(a.x, cy.U[0].x); L.U[1] = v2(a.y, cy.U[1].x);
-      L.U[2] = v2(a.z, cy.U[2].x); L.U[3] = v2(a.w, cy.U[3].x);
-      L.U[4] = v2(b.x, cy.U[4].x); L.F[0] = v2(b.y, cy.F[0].x);
-      L.F[1] = v2(b.z, cy.F[1].x); L.F[2] = v2(b.w, cy.F[2].x);
-      L.F[3] = v2(d.x, cy.F[3].x); L.F[4] = v2(d.y, cy.F[4].x);
-      L.u = v2(d.z, cy.u.x);       L.c = v2(d.w, cy.c.x);
-    }
-    V2 fy[5];
-    P::hll(L, cy, fy);
-    sm.fy4[w][lane] = make_float4(fy[0].x, fy[1].x, fy[2].x, fy[3].x);
-    sm.fy1[w][lane] = fy[4].x;
-    __syncthreads();
-    V2 fyh[5];
-    {
-      float4 f4;
-      float f1;
-      if (w <= NWP - 2) {
-        f4 = sm.fy4[w + 1][lane];
-        f1 = sm.fy1[w + 1][lane];
-      } else {
-        f4 = make_float4(fy[0].x, fy[1].x, fy[2].x, fy[3].x);
-        f1 = fy[4].x;
-      }
-      fyh[0] = v2(fy[0].y, f4.x);
-      fyh[1] = v2(fy[1].y, f4.y);
-      fyh[2] = v2(fy[2].y, f4.z);
-      fyh[3] = v2(fy[3].y, f4.w);
-      fyh[4] = v2(fy[4].y, f1);
-    }
-    V2 s2[5];
-    P::update(cy, fy, fyh, s2, K);
-    // ---- barrier-free block: z sweep of x and x sweep of x+1 ----
+    for (int i = 0; i < 5; ++i) f0[i] = f1[i];
     if (x + 1 < t.x_end) {
-      x_sweep(pf, s1);
-      if (x + 4 <= t.x_end) load(x + 4, pf);
-    }
-    Cell2 cz, nb;
-    P::template derive<3>(s2, cz, K);
-    shfl_up_cell2(cz, nb);
-    V2 fzl[5], fzh[5];
-    P::hll(nb, cz, fzl);
+      plane_update<P, NWP, IDX32>(x + 1, pa, c0, f0, c1, f1, K, sm, o,
+                                  [&]() { if (x + 4 <= t.x_end) load(x + 4, pa); }, sync_only);
+      c0 = c1;
 #pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      fzh[i].x = __shfl_down_sync(0xffffffffu, fzl[i].x, 1);
-      fzh[i].y = __shfl_down_sync(0xffffffffu, fzl[i].y, 1);
+      for (int i = 0; i < 5; ++i) f0[i] = f1[i];
     }
-    V2 s3[5], wo[5];
-    P::update(cz, fzl, fzh, s3, K);
-    const V2 sp = P::finish(s3, wo, K);
-    float* q = o.dst + (size_t)x * o.plane;
-    if (o.store_a) {
-#pragma unroll
-      for (int i = 0; i < 5; ++i) q[i * o.vstride + o.dcol_a] = wo[i].x;
-      o.wmax = speed_max(o.wmax, sp.x);
-    }
-    if (o.store_b) {
-#pragma unroll
-      for (int i = 0; i < 5; ++i) q[i * o.vstride + o.dcol_b] = wo[i].y;
-      o.wmax = speed_max(o.wmax, sp.y);
-    }
-  };
-  // planes x+2 alternate between pb (x even offset) and pa
-  for (int x = t.x0; x < t.x_end; x += 2) {
-    trip(x, pb);
-    if (x + 1 < t.x_end) trip(x + 1, pa);
+#else  // the two carries alternate roles
+    plane_update<P, NWP, IDX32>(x, pb, c0, f0, c1, f1, K, sm, o,
+                                [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); }, sync_only);
+    if (x + 1 < t.x_end)
+      plane_update<P, NWP, IDX32>(x + 1, pa, c1, f1, c0, f0, K, sm, o,
+                                  [&]() { if (x + 4 <= t.x_end) load(x + 4, pa); }, sync_only);
+#endif
   }
   return o.wmax;
 }
@@ -573,19 +460,17 @@ __device__ __forceinline__ float fused_tile_tma(const float* __restrict__ src,
     }
   };
 
-  Cell2 cur;
-  V2 fm[5];
+  Cell2 c0, c1;  // carried plane quantities, alternating roles
+  V2 f0[5], f1[5];
   {
     V2 w0[5], w1[5], s[5];
     read(0, w0);
     read(1, w1);
     P::to_state(w0, s, K);
-    P::template derive<1>(s, cur, K);
-    Cell2 nx_;
+    P::template derive<1>(s, c1, K);
     P::to_state(w1, s, K);
-    P::template derive<1>(s, nx_, K);
-    P::hll(cur, nx_, fm);  // flux at face x0 - 1/2
-    cur = nx_;
+    P::template derive<1>(s, c0, K);
+    P::hll(c1, c0, f0);  // flux at face x0 - 1/2; c0 = plane x0
   }
   if (__syncthreads_or(bad)) {
     *timed_out = true;
@@ -594,12 +479,12 @@ __device__ __forceinline__ float fused_tile_tma(const float* __restrict__ src,
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       for (int r = kStages; r < kStages + 2 && r <= L; ++r) issue(r);
     }
-    for (int x = t.x0; x < t.x_end; ++x) {
+    auto step = [&](int x, const Cell2& cur, const V2* fm, Cell2& nxt, V2* fp) {
       const int r = x - t.x0 + 2;  // plane x+1
       V2 pf[5];
       read(r, pf);
-      const bool stop = plane_update<P, NWP>(
-          x, pf, cur, fm, K, sm, o, []() {},
+      return plane_update<P, NWP, false>(
+          x, pf, cur, fm, nxt, fp, K, sm, o, []() {},
           [&]() {
             if (__syncthreads_or(bad)) return true;
             if (threadIdx.x == 0 && r + kStages <= L) {
@@ -608,7 +493,13 @@ __device__ __forceinline__ float fused_tile_tma(const float* __restrict__ src,
             }
             return false;
           });
-      if (stop) {
+    };
+    for (int x = t.x0; x < t.x_end; x += 2) {
+      if (step(x, c0, f0, c1, f1)) {
+        *timed_out = true;
+        break;
+      }
+      if (x + 1 < t.x_end && step(x + 1, c1, f1, c0, f0)) {
         *timed_out = true;
         break;
       }

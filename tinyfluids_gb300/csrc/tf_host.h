@@ -25,7 +25,7 @@ int sm_count();  // multiprocessors of the current device (cached per device)
 
 // Tile heights (grid rows incl. the one-cell ring) the fused kernel is
 // instantiated for; the kernel uses rows/2 warps.
-inline bool valid_tile_rows(int rows) { return rows == 8 || rows == 16 || rows == 32 || rows == 34; }
+inline bool valid_tile_rows(int rows) { return rows == 8 || rows == 16 || rows == 32; }
 
 // CTAs per SM the fused kernels are register-bounded for: TF_WARPS_PER_SM
 // (16 by default) warps per SM for every tile height.
@@ -46,12 +46,8 @@ __host__ __device__ constexpr int min_ctas_per_sm(int nwp) {
       constexpr int NWP = 8;                      \
       __VA_ARGS__;                                \
     } break;                                      \
-    case 32: {                                    \
-      constexpr int NWP = 16;                     \
-      __VA_ARGS__;                                \
-    } break;                                      \
     default: {                                    \
-      constexpr int NWP = 17;                     \
+      constexpr int NWP = 16;                     \
       __VA_ARGS__;                                \
     } break;                                      \
   }

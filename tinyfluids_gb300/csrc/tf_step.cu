@@ -163,7 +163,7 @@ struct FusedArgs {
   int loop;        // 1: predicated loop step (parity buffers, dt from ctl)
 };
 
-template <class P, int NWP, bool PIPELINED = false>
+template <class P, int NWP, bool IDX32>
 __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_kernel(FusedArgs a) {
   __shared__ FusedSmem<NWP> sm;
   const float* src;
@@ -187,10 +187,8 @@ __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_ker
   K.inv_dx = a.inv_dx;
   K.dt = dt;
   K.k = dt * a.inv_dx;
-  float m = PIPELINED ? fused_tile_pipelined<P, NWP>(src, dst, a.geo, blockIdx.x, blockIdx.y,
-                                                     blockIdx.z, K, sm)
-                      : fused_tile<P, NWP>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z, K,
-                                           sm);
+  float m = fused_tile<P, NWP, false, IDX32>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z,
+                                             K, sm);
   if (a.ctl) {
     float bm = block_max(m, sm.red);
     if (threadIdx.x == 0)
@@ -338,13 +336,12 @@ static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx, int* loa
   *loader = 0;
   if (tile) {
     if (!valid_tile_rows(tile->rows))
-      return set_error(TF_ERR_ARG, "tile rows must be 8, 16, 32 or 34 (got %d)", tile->rows);
+      return set_error(TF_ERR_ARG, "tile rows must be 8, 16 or 32 (got %d)", tile->rows);
     *rows = tile->rows;
     *lx = tile->lx;
     if (*lx < 0) return set_error(TF_ERR_ARG, "tile lx must be >= 0");
-    if (tile->loader < 0 || tile->loader > 3)
-      return set_error(TF_ERR_ARG,
-                       "tile loader must be 0 (auto), 1 (loads), 2 (TMA) or 3 (pipelined loads)");
+    if (tile->loader < 0 || tile->loader > 2)
+      return set_error(TF_ERR_ARG, "tile loader must be 0 (auto), 1 (loads) or 2 (TMA)");
     *loader = tile->loader;
   }
   return TF_OK;
@@ -353,9 +350,7 @@ static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx, int* loa
 template <int NWP>
 static int launch_tma(const FusedArgs& a, dim3 grid, const CUtensorMap* tm, bool exact,
                       cudaStream_t s) {
-  if constexpr (NWP == 17) {
-    return set_error(TF_ERR_UNSUPPORTED, "TMA planes need 8, 16 or 32 tile rows");
-  } else {
+  {
     const size_t smem = tma_smem_bytes(NWP) + 128;
     auto k = exact ? fused_step_tma_kernel<ExactPair, NWP> : fused_step_tma_kernel<FastPair, NWP>;
     TF_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -385,16 +380,20 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
       return launch_check("fused_step_tma_kernel");
     }
   }
-  if (loader == 3) {
-    TF_DISPATCH_ROWS(rows, NWP, {
-      if (exact) fused_step_kernel<ExactPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
-      else fused_step_kernel<FastPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
-    });
-    return launch_check("fused_step_kernel");
-  }
+  // 32-bit element offsets when the state has fewer than 2^31 floats
+#ifdef TF_NO_IDX32
+  const bool idx32 = false;
+#else
+  const bool idx32 = 5ull * a.geo.nx * a.geo.ny * a.geo.nz < 0x7fffffffull;
+#endif
   TF_DISPATCH_ROWS(rows, NWP, {
-    if (exact) fused_step_kernel<ExactPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
-    else fused_step_kernel<FastPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
+    if (exact) {
+      if (idx32) fused_step_kernel<ExactPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
+      else fused_step_kernel<ExactPair, NWP, false><<<grid, NWP * 32, 0, s>>>(a);
+    } else {
+      if (idx32) fused_step_kernel<FastPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
+      else fused_step_kernel<FastPair, NWP, false><<<grid, NWP * 32, 0, s>>>(a);
+    }
   });
   return launch_check("fused_step_kernel");
 }
