@@ -291,6 +291,29 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
   };
   // Two planes per trip so the prefetch buffers alternate without moves;
   // `pf` holds plane x+1 on entry and receives plane x+3.
+#ifdef TF_CARRY_U
+  // carry only the conserved state of plane x and re-derive its cell each
+  // plane (fewer live registers, one more derive per plane)
+  V2 u0[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) u0[i] = c0.U[i];
+  for (int x = t.x0; x < t.x_end; ++x) {
+    V2* pf = ((x - t.x0) & 1) ? pa : pb;
+    P::template derive<1>(u0, c0, K);
+    plane_update<P, NWP, IDX32>(
+        x, pf, c0, f0, c1, f1, K, sm, o,
+        [&]() {
+          if (x + 3 <= t.x_end) load(x + 3, pf);
+        },
+        sync_only);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      u0[i] = c1.U[i];
+      f0[i] = f1[i];
+    }
+  }
+  if (false)
+#endif
   for (int x = t.x0; x < t.x_end; x += 2) {
 #ifndef TF_CARRY_PINGPONG  // the carry is copied back after each plane (fewer live registers)
     plane_update<P, NWP, IDX32>(x, pb, c0, f0, c1, f1, K, sm, o,

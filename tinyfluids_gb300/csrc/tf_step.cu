@@ -381,10 +381,12 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
     }
   }
   // 32-bit element offsets when the state has fewer than 2^31 floats
-#ifdef TF_NO_IDX32
-  const bool idx32 = false;
-#else
+#ifdef TF_IDX32
   const bool idx32 = 5ull * a.geo.nx * a.geo.ny * a.geo.nz < 0x7fffffffull;
+#else
+  // 32-bit offsets cut the integer ops but measured slower (the kernel sits at
+  // its register cap and the saved registers turn into moves)
+  const bool idx32 = false;
 #endif
   TF_DISPATCH_ROWS(rows, NWP, {
     if (exact) {
