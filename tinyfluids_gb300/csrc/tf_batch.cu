@@ -56,7 +56,6 @@ struct BatchPlan {  // host mirror of a prepared workspace
   unsigned long long wait_limit = 0;
   int tiles_per_step = 0;
   int chunks_total = 0;
-  int idx32 = 1;  // every instance has fewer than 2^31 floats
 };
 
 static std::mutex g_plan_mu;
@@ -172,7 +171,7 @@ __device__ __forceinline__ void tile_coords(const FusedGeom& g, int t, int& tz, 
 }
 
 // One step of every active instance: one CTA per (instance, tile).
-template <class P, int NWP, bool IDX32>
+template <class P, int NWP>
 __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) batch_step_kernel(const BatchInst* __restrict__ inst,
                                                                 const int* __restrict__ tile_prefix,
                                                                 int count) {
@@ -189,7 +188,7 @@ __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) batch_step_ker
   setup_step(I, iter, dt, src, dst, K);
   int tz, ty, tx;
   tile_coords(I.geo, r - __ldg(tile_prefix + i), tz, ty, tx);
-  float m = fused_tile<P, NWP, false, IDX32>(src, dst, I.geo, tz, ty, tx, K, sm);
+  float m = fused_tile<P, NWP, false>(src, dst, I.geo, tz, ty, tx, K, sm);
   float bm = block_max(m, sm.red);
   if (threadIdx.x == 0) ctl_finish_cta(I.ctl, bm, (unsigned)I.ntiles, dt, true);
 }
@@ -201,7 +200,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // All steps of all instances in one launch (see the file comment).
-template <class P, int NWP, bool IDX32>
+template <class P, int NWP>
 __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP))
     batch_persistent_kernel(BatchHeader* hdr, const BatchInst* __restrict__ inst,
                             const int* __restrict__ tile_prefix, int count, int tiles_per_step,
@@ -257,7 +256,7 @@ __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP))
     setup_step(I, s_iter, dt, src, dst, K);
     int tz, ty, tx;
     tile_coords(I.geo, r - __ldg(tile_prefix + i), tz, ty, tx);
-    float m = fused_tile<P, NWP, true, IDX32>(src, dst, I.geo, tz, ty, tx, K, sm);
+    float m = fused_tile<P, NWP, true>(src, dst, I.geo, tz, ty, tx, K, sm);
     __threadfence();  // this thread's stores before the CTA's completion count
     float bm = block_max(m, sm.red);
     if (threadIdx.x == 0) ctl_finish_cta(I.ctl, bm, (unsigned)I.ntiles, dt, true);
@@ -265,14 +264,14 @@ __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP))
   }
 }
 
-template <class P, int NWP, bool IDX32>
+template <class P, int NWP>
 static int occupancy_persistent(int* per_sm) {
   return cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                        per_sm, batch_persistent_kernel<P, NWP, IDX32>, NWP * 32, 0),
+                        per_sm, batch_persistent_kernel<P, NWP>, NWP * 32, 0),
                     "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
 }
 
-template <class P, int NWP, bool IDX32>
+template <class P, int NWP>
 static int launch_batch(const BatchPlan& p, void* ws, int step_base, int steps, cudaStream_t s) {
   Layout L = layout(p.count);
   char* base = (char*)ws;
@@ -282,7 +281,7 @@ static int launch_batch(const BatchPlan& p, void* ws, int step_base, int steps, 
   if (p.persistent) {
     int per_sm = p.ctas_per_sm;
     if (per_sm <= 0) {
-      TF_TRY((occupancy_persistent<P, NWP, IDX32>(&per_sm)));
+      TF_TRY((occupancy_persistent<P, NWP>(&per_sm)));
       if (per_sm < 1) per_sm = 1;
     }
     long long grid = (long long)per_sm * sm_count();
@@ -290,12 +289,12 @@ static int launch_batch(const BatchPlan& p, void* ws, int step_base, int steps, 
     if (grid > total) grid = total;
     if (grid < 1) return TF_OK;
     unsigned long long lim = p.wait_limit ? p.wait_limit : (1ull << 24);
-    batch_persistent_kernel<P, NWP, IDX32><<<(int)grid, NWP * 32, 0, s>>>(
+    batch_persistent_kernel<P, NWP><<<(int)grid, NWP * 32, 0, s>>>(
         hdr, inst, tp, p.count, p.tiles_per_step, step_base, steps, lim);
     return launch_check("batch_persistent_kernel");
   }
   for (int k = 0; k < steps; ++k) {
-    batch_step_kernel<P, NWP, IDX32><<<p.tiles_per_step, NWP * 32, 0, s>>>(inst, tp, p.count);
+    batch_step_kernel<P, NWP><<<p.tiles_per_step, NWP * 32, 0, s>>>(inst, tp, p.count);
     TF_TRY(launch_check("batch_step_kernel"));
   }
   return TF_OK;
@@ -380,7 +379,6 @@ int tf_batch_prepare(const tf_instance* inst, int count, const tf_batch_config* 
     b.t_final = q.t_final;
     b.max_steps = q.max_steps;
     b.ncells = (long long)q.nx * q.ny * q.nz;
-    if (5 * b.ncells >= 0x7fffffffLL) plan.idx32 = 0;
     long long nt = (long long)g.tiles_z * g.tiles_y * g.tiles_x;
     b.ntiles = (int)nt;
     b.nchunks = (int)((b.ncells + kChunkCells - 1) / kChunkCells);
@@ -436,13 +434,8 @@ int tf_batch_run(void* workspace, int step_base, int steps, void* stream) {
     TF_TRY(cuda_check(cudaMemsetAsync(hdr, 0, sizeof(unsigned long long), s), "cudaMemsetAsync"));
   }
   TF_DISPATCH_ROWS(p.rows, NWP, {
-    if (p.exact) {
-      if (p.idx32) TF_TRY((launch_batch<ExactPair, NWP, true>(p, workspace, step_base, steps, s)));
-      else TF_TRY((launch_batch<ExactPair, NWP, false>(p, workspace, step_base, steps, s)));
-    } else {
-      if (p.idx32) TF_TRY((launch_batch<FastPair, NWP, true>(p, workspace, step_base, steps, s)));
-      else TF_TRY((launch_batch<FastPair, NWP, false>(p, workspace, step_base, steps, s)));
-    }
+    if (p.exact) TF_TRY((launch_batch<ExactPair, NWP>(p, workspace, step_base, steps, s)));
+    else TF_TRY((launch_batch<FastPair, NWP>(p, workspace, step_base, steps, s)));
   });
   batch_final_kernel<<<grid_chunks, 256, 0, s>>>(inst, cp, p.count, p.chunks_total);
   return launch_check("batch_final_kernel");

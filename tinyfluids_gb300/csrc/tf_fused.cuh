@@ -79,21 +79,11 @@ struct TileOut {
   float wmax;
 };
 
-// Element offsets are 32-bit (IDX32) when the whole state has fewer than
-// 2^31 floats, which halves the address arithmetic of every access.
-template <bool IDX32>
 __device__ __forceinline__ void store5(const TileOut& o, int x, size_t dcol, const V2 wo[5],
                                        bool hi) {
-  if (IDX32) {
-    const unsigned base = (unsigned)x * (unsigned)o.plane + (unsigned)dcol;
-    const unsigned vs = (unsigned)o.vstride;
+  float* q = o.dst + (size_t)x * o.plane + dcol;
 #pragma unroll
-    for (int i = 0; i < 5; ++i) o.dst[base + (unsigned)i * vs] = hi ? wo[i].y : wo[i].x;
-  } else {
-    float* q = o.dst + (size_t)x * o.plane + dcol;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) q[i * o.vstride] = hi ? wo[i].y : wo[i].x;
-  }
+  for (int i = 0; i < 5; ++i) q[i * o.vstride] = hi ? wo[i].y : wo[i].x;
 }
 
 // One plane of the fused step for the thread's pair of cells: the x sweep
@@ -103,7 +93,7 @@ __device__ __forceinline__ void store5(const TileOut& o, int x, size_t dcol, con
 // `after_sync()` runs after the plane's first CTA barrier, when every thread
 // has read plane x+1 (the TMA loader refills its stage there) and returns
 // true if the CTA must stop (a bounded wait gave up).
-template <class P, int NWP, bool IDX32, class Consumed, class AfterSync>
+template <class P, int NWP, class Consumed, class AfterSync>
 __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, const V2 fm[5],
                                              Cell2& nxt, V2 fp[5], const StepConsts<float>& K,
                                              FusedSmem<NWP>& sm, TileOut& o, Consumed consumed,
@@ -191,11 +181,11 @@ __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, 
   P::update(cz, fzl, fzh, s3, K);
   const V2 sp = P::finish(s3, wo, K);
   if (o.store_a) {
-    store5<IDX32>(o, x, o.dcol_a, wo, false);
+    store5(o, x, o.dcol_a, wo, false);
     o.wmax = speed_max(o.wmax, sp.x);
   }
   if (o.store_b) {
-    store5<IDX32>(o, x, o.dcol_b, wo, true);
+    store5(o, x, o.dcol_b, wo, true);
     o.wmax = speed_max(o.wmax, sp.y);
   }
   return stop;
@@ -241,36 +231,26 @@ __device__ __forceinline__ TileCols tile_cols(const FusedGeom& G, int tz, int ty
 // L2-only loads (ld.global.cg) for kernels that read data other CTAs wrote
 // earlier in the same launch (the persistent batch kernel); otherwise loads
 // use the read-only path.
-template <class P, int NWP, bool COHERENT = false, bool IDX32 = false>
+template <class P, int NWP, bool COHERENT = false>
 __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float* __restrict__ dst,
                                             const FusedGeom& G, int tz, int ty, int tx,
                                             const StepConsts<float>& K, FusedSmem<NWP>& sm) {
   TileOut o;
   const TileCols t = tile_cols<NWP>(G, tz, ty, tx, src, dst, o);
   const bool open = G.open_bc != 0;
-  const unsigned vs32 = (unsigned)o.vstride, pl32 = (unsigned)o.plane;
-  const unsigned ca32 = (unsigned)t.col_a, cb32 = (unsigned)t.col_b;
   auto ld = [&](const float* p) { return COHERENT ? __ldcg(p) : __ldg(p); };
   auto load = [&](int x, V2 v[5]) {
-    const int xs = src_index(x, G.nx, open);
-    if (IDX32) {
-      const unsigned po = (unsigned)xs * pl32;
+    const float* p = src + (size_t)src_index(x, G.nx, open) * o.plane;
 #pragma unroll
-      for (int i = 0; i < 5; ++i) {
-        v[i].x = ld(src + (po + ca32 + (unsigned)i * vs32));
-        v[i].y = ld(src + (po + cb32 + (unsigned)i * vs32));
-      }
-    } else {
-      const float* p = src + (size_t)xs * o.plane;
-#pragma unroll
-      for (int i = 0; i < 5; ++i) {
-        const float* q = p + i * o.vstride;
-        v[i].x = ld(q + t.col_a);
-        v[i].y = ld(q + t.col_b);
-      }
+    for (int i = 0; i < 5; ++i) {
+      const float* q = p + i * o.vstride;
+      v[i].x = ld(q + t.col_a);
+      v[i].y = ld(q + t.col_b);
     }
   };
-  Cell2 c0, c1;  // carried plane quantities, alternating roles
+  // carried plane quantities: c0 = plane x, c1 receives plane x+1 (copying
+  // it back measured fewer live registers than alternating the two roles)
+  Cell2 c0, c1;
   V2 f0[5], f1[5];
   V2 pa[5], pb[5];
   {
@@ -291,50 +271,19 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
   };
   // Two planes per trip so the prefetch buffers alternate without moves;
   // `pf` holds plane x+1 on entry and receives plane x+3.
-#ifdef TF_CARRY_U
-  // carry only the conserved state of plane x and re-derive its cell each
-  // plane (fewer live registers, one more derive per plane)
-  V2 u0[5];
-#pragma unroll
-  for (int i = 0; i < 5; ++i) u0[i] = c0.U[i];
-  for (int x = t.x0; x < t.x_end; ++x) {
-    V2* pf = ((x - t.x0) & 1) ? pa : pb;
-    P::template derive<1>(u0, c0, K);
-    plane_update<P, NWP, IDX32>(
-        x, pf, c0, f0, c1, f1, K, sm, o,
-        [&]() {
-          if (x + 3 <= t.x_end) load(x + 3, pf);
-        },
-        sync_only);
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      u0[i] = c1.U[i];
-      f0[i] = f1[i];
-    }
-  }
-  if (false)
-#endif
   for (int x = t.x0; x < t.x_end; x += 2) {
-#ifndef TF_CARRY_PINGPONG  // the carry is copied back after each plane (fewer live registers)
-    plane_update<P, NWP, IDX32>(x, pb, c0, f0, c1, f1, K, sm, o,
-                                [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); }, sync_only);
+    plane_update<P, NWP>(x, pb, c0, f0, c1, f1, K, sm, o,
+                         [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); }, sync_only);
     c0 = c1;
 #pragma unroll
     for (int i = 0; i < 5; ++i) f0[i] = f1[i];
     if (x + 1 < t.x_end) {
-      plane_update<P, NWP, IDX32>(x + 1, pa, c0, f0, c1, f1, K, sm, o,
-                                  [&]() { if (x + 4 <= t.x_end) load(x + 4, pa); }, sync_only);
+      plane_update<P, NWP>(x + 1, pa, c0, f0, c1, f1, K, sm, o,
+                           [&]() { if (x + 4 <= t.x_end) load(x + 4, pa); }, sync_only);
       c0 = c1;
 #pragma unroll
       for (int i = 0; i < 5; ++i) f0[i] = f1[i];
     }
-#else  // the two carries alternate roles
-    plane_update<P, NWP, IDX32>(x, pb, c0, f0, c1, f1, K, sm, o,
-                                [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); }, sync_only);
-    if (x + 1 < t.x_end)
-      plane_update<P, NWP, IDX32>(x + 1, pa, c1, f1, c0, f0, K, sm, o,
-                                  [&]() { if (x + 4 <= t.x_end) load(x + 4, pa); }, sync_only);
-#endif
   }
   return o.wmax;
 }
@@ -506,7 +455,7 @@ __device__ __forceinline__ float fused_tile_tma(const float* __restrict__ src,
       const int r = x - t.x0 + 2;  // plane x+1
       V2 pf[5];
       read(r, pf);
-      return plane_update<P, NWP, false>(
+      return plane_update<P, NWP>(
           x, pf, cur, fm, nxt, fp, K, sm, o, []() {},
           [&]() {
             if (__syncthreads_or(bad)) return true;

@@ -163,7 +163,7 @@ struct FusedArgs {
   int loop;        // 1: predicated loop step (parity buffers, dt from ctl)
 };
 
-template <class P, int NWP, bool IDX32>
+template <class P, int NWP>
 __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_kernel(FusedArgs a) {
   __shared__ FusedSmem<NWP> sm;
   const float* src;
@@ -187,8 +187,7 @@ __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_ker
   K.inv_dx = a.inv_dx;
   K.dt = dt;
   K.k = dt * a.inv_dx;
-  float m = fused_tile<P, NWP, false, IDX32>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z,
-                                             K, sm);
+  float m = fused_tile<P, NWP>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z, K, sm);
   if (a.ctl) {
     float bm = block_max(m, sm.red);
     if (threadIdx.x == 0)
@@ -315,9 +314,10 @@ static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int
   g.tiles_z = (nz + kTileZ - 1) / kTileZ;
   g.tiles_y = (ny + (rows - 2) - 1) / (rows - 2);
   if (lx <= 0) {
-    // enough CTAs for ~8 waves of resident CTAs, chunks of >= 8 planes
+    // enough CTAs for ~12 waves of resident CTAs, chunks of >= 8 planes
+    // (512^3, 16-row tiles: 6 chunks of 86 planes)
     long long tiles_yz = (long long)g.tiles_z * g.tiles_y;
-    long long want = 8LL * sm_count() * min_ctas_per_sm(rows / 2);
+    long long want = 12LL * sm_count() * min_ctas_per_sm(rows / 2);
     long long tx = (want + tiles_yz - 1) / tiles_yz;
     long long max_tx = nx / 8 > 0 ? nx / 8 : 1;
     if (tx > max_tx) tx = max_tx;
@@ -381,21 +381,9 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
     }
   }
   // 32-bit element offsets when the state has fewer than 2^31 floats
-#ifdef TF_IDX32
-  const bool idx32 = 5ull * a.geo.nx * a.geo.ny * a.geo.nz < 0x7fffffffull;
-#else
-  // 32-bit offsets cut the integer ops but measured slower (the kernel sits at
-  // its register cap and the saved registers turn into moves)
-  const bool idx32 = false;
-#endif
   TF_DISPATCH_ROWS(rows, NWP, {
-    if (exact) {
-      if (idx32) fused_step_kernel<ExactPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
-      else fused_step_kernel<ExactPair, NWP, false><<<grid, NWP * 32, 0, s>>>(a);
-    } else {
-      if (idx32) fused_step_kernel<FastPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
-      else fused_step_kernel<FastPair, NWP, false><<<grid, NWP * 32, 0, s>>>(a);
-    }
+    if (exact) fused_step_kernel<ExactPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
+    else fused_step_kernel<FastPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
   });
   return launch_check("fused_step_kernel");
 }
