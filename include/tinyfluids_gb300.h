@@ -240,7 +240,8 @@ int tf_batch_error(void *workspace, int *error_host, void *stream);
 /* Forgets the host-side plan of a workspace. */
 int tf_batch_release(void *workspace);
 
-/* ---- initial states, built on the device (W: 5*n^3 floats, n^3 grid) ---- */
+/* ---- initial states, built on the device (W: 5*n^3 floats, n^3 grid,
+ * 1 <= n <= 65535; computed in float32) ---- */
 
 /* scaling_jax.py:23-41 setup_ics(n, k): rho = 0.125, p = 0.1, u = 0; rho = p = 1
  * on [n/2-k, n/2+k)^3.  The caller uses dx = 1/(n-1) like the reference. */

@@ -3,8 +3,9 @@
 ``setup_ics`` restates scaling_jax.py:23-41 (the reference's injection cube).
 ``overpressure`` and ``shear_layer`` are the two benchmark initial states
 (spherical overpressure; shear layer with a seeded vy perturbation), built on
-the host with the same seeded generator the product's builders use, so a test
-can hand both sides bit-identical inputs.
+the host with numpy's seeded generator.  They follow the same formulas as the
+device builders but not the same random draws; a test hands one array to both
+the oracle and the GPU path.
 """
 from __future__ import annotations
 

@@ -99,7 +99,7 @@ __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, 
                                              FusedSmem<NWP>& sm, TileOut& o, Consumed consumed,
                                              AfterSync after_sync) {
   // cur / fm: plane x and the flux at x-1/2; nxt / fp receive plane x+1 and
-  // the flux at x+1/2 (the caller alternates two carries instead of copying)
+  // the flux at x+1/2 (the caller copies them into cur / fm for the next plane)
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   V2 s[5];

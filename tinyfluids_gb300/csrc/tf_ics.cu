@@ -19,26 +19,41 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   return x ^ (x >> 31);
 }
 
-// Uniform double in [0, 1) from 53 hash bits.
-__device__ __forceinline__ double hash_uniform(uint64_t seed, uint64_t stream, uint64_t i) {
+// Uniform float in [0, 1) from the top 24 hash bits.
+__device__ __forceinline__ float hash_uniform(uint64_t seed, uint64_t stream, uint64_t i) {
   uint64_t h = mix64(mix64(seed ^ (stream * 0xD1B54A32D192ED03ull)) + i);
-  return (double)(h >> 11) * (1.0 / 9007199254740992.0);
+  return (float)(h >> 40) * (1.0f / 16777216.0f);
 }
 
-// Standard normal by Box-Muller from two hash uniforms.
-__device__ __forceinline__ double hash_normal(uint64_t seed, uint64_t stream, uint64_t i) {
-  double u1 = hash_uniform(seed, stream, 2 * i);
-  double u2 = hash_uniform(seed, stream, 2 * i + 1);
-  u1 = 1.0 - u1;  // (0, 1]
-  return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+// Standard normal by Box-Muller from two hash uniforms (float32: the fill is
+// bandwidth-bound, and GB300's FP64 rate is a small fraction of its FP32 rate).
+__device__ __forceinline__ float hash_normal(uint64_t seed, uint64_t stream, uint64_t i) {
+  float u1 = 1.0f - hash_uniform(seed, stream, 2 * i);  // (0, 1]
+  float u2 = hash_uniform(seed, stream, 2 * i + 1);
+  return sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+}
+
+// Launch shape of the fills: blockIdx.y = y row, blockIdx.z = x plane,
+// threads stride over z -- no index division per cell.
+struct FillIdx {
+  int x, y;
+  long long row;  // linear index of (x, y, 0)
+};
+__device__ __forceinline__ FillIdx fill_idx(int n) {
+  FillIdx f;
+  f.y = blockIdx.y;
+  f.x = blockIdx.z;
+  f.row = ((long long)f.x * n + f.y) * n;
+  return f;
 }
 
 __global__ void ics_cube_kernel(float* W, int n, int lo, int hi) {
-  long long n3 = (long long)n * n * n;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
-       i += (long long)gridDim.x * blockDim.x) {
-    int z = (int)(i % n), y = (int)((i / n) % n), x = (int)(i / ((long long)n * n));
-    bool in = x >= lo && x < hi && y >= lo && y < hi && z >= lo && z < hi;
+  const long long n3 = (long long)n * n * n;
+  const FillIdx f = fill_idx(n);
+  const bool in_xy = f.x >= lo && f.x < hi && f.y >= lo && f.y < hi;
+  for (int z = threadIdx.x; z < n; z += blockDim.x) {
+    const long long i = f.row + z;
+    const bool in = in_xy && z >= lo && z < hi;
     W[i] = in ? 1.0f : 0.125f;
     W[n3 + i] = 0.f;
     W[2 * n3 + i] = 0.f;
@@ -47,44 +62,52 @@ __global__ void ics_cube_kernel(float* W, int n, int lo, int hi) {
   }
 }
 
-__global__ void ics_overpressure_kernel(float* W, int n, uint64_t seed, double radius, double p_in,
-                                        double p_out, double rho0, double noise) {
-  long long n3 = (long long)n * n * n;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
-       i += (long long)gridDim.x * blockDim.x) {
-    int z = (int)(i % n), y = (int)((i / n) % n), x = (int)(i / ((long long)n * n));
-    double cx = (x + 0.5) / n - 0.5, cy = (y + 0.5) / n - 0.5, cz = (z + 0.5) / n - 0.5;
-    double r2 = cx * cx + cy * cy + cz * cz;
-    double u = hash_uniform(seed, 1, (uint64_t)i);
-    W[i] = (float)(rho0 * (1.0 + noise * (2.0 * u - 1.0)));
+__global__ void ics_overpressure_kernel(float* W, int n, uint64_t seed, float radius, float p_in,
+                                        float p_out, float rho0, float noise) {
+  const long long n3 = (long long)n * n * n;
+  const FillIdx f = fill_idx(n);
+  const float inv_n = 1.0f / (float)n;
+  const float cx = (f.x + 0.5f) * inv_n - 0.5f, cy = (f.y + 0.5f) * inv_n - 0.5f;
+  const float r2xy = cx * cx + cy * cy;
+  for (int z = threadIdx.x; z < n; z += blockDim.x) {
+    const long long i = f.row + z;
+    const float cz = (z + 0.5f) * inv_n - 0.5f;
+    const float r2 = r2xy + cz * cz;
+    const float u = hash_uniform(seed, 1, (uint64_t)i);
+    W[i] = rho0 * (1.0f + noise * (2.0f * u - 1.0f));
     W[n3 + i] = 0.f;
     W[2 * n3 + i] = 0.f;
     W[3 * n3 + i] = 0.f;
-    W[4 * n3 + i] = (float)(r2 < radius * radius ? p_in : p_out);
+    W[4 * n3 + i] = r2 < radius * radius ? p_in : p_out;
   }
 }
 
-__global__ void ics_shear_kernel(float* W, int n, uint64_t seed, double amplitude) {
-  long long n3 = (long long)n * n * n;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
-       i += (long long)gridDim.x * blockDim.x) {
-    int y = (int)((i / n) % n), x = (int)(i / ((long long)n * n));
-    double yc = (y + 0.5) / n, xc = (x + 0.5) / n;
-    bool band = fabs(yc - 0.5) < 0.25;
-    double a = hash_normal(seed, 2, (uint64_t)i);
+__global__ void ics_shear_kernel(float* W, int n, uint64_t seed, float amplitude) {
+  const long long n3 = (long long)n * n * n;
+  const FillIdx f = fill_idx(n);
+  const float inv_n = 1.0f / (float)n;
+  const float yc = (f.y + 0.5f) * inv_n, xc = (f.x + 0.5f) * inv_n;
+  const bool band = fabsf(yc - 0.5f) < 0.25f;
+  const float vy_scale = amplitude * sinpif(4.0f * xc);
+  for (int z = threadIdx.x; z < n; z += blockDim.x) {
+    const long long i = f.row + z;
+    const float a = hash_normal(seed, 2, (uint64_t)i);
     W[i] = band ? 2.0f : 1.0f;
     W[n3 + i] = band ? 0.5f : -0.5f;
-    W[2 * n3 + i] = (float)(amplitude * sinpi(4.0 * xc) * a);
+    W[2 * n3 + i] = vy_scale * a;
     W[3 * n3 + i] = 0.f;
     W[4 * n3 + i] = 2.5f;
   }
 }
 
-static int ics_grid(long long n3) {
-  long long b = (n3 + 255) / 256;
-  long long cap = (long long)sm_count() * 16;
-  return (int)(b < 1 ? 1 : (b < cap ? b : cap));
+static dim3 fill_grid(int n) { return dim3(1, (unsigned)n, (unsigned)n); }
+static int fill_threads(int n) { return n >= 256 ? 256 : ((n + 31) / 32) * 32; }
+static int check_fill(float* W, int n) {
+  if (!W || n < 1) return set_error(TF_ERR_ARG, "bad arguments");
+  if (n > 65535) return set_error(TF_ERR_ARG, "grid size %d above 65535", n);
+  return TF_OK;
 }
+
 
 }  // namespace tf
 
@@ -95,15 +118,14 @@ extern "C" {
 // scaling_jax.py:23-41 setup_ics: rho = 0.125, p = 0.1, u = 0, and rho = p = 1
 // on the cube [n/2 - k, n/2 + k)^3.  W: 5*n^3 floats.
 int tf_ics_injection_cube(float* W, int n, int num_injection_cells, void* stream) {
-  if (!W || n < 1) return set_error(TF_ERR_ARG, "bad arguments");
+  TF_TRY(check_fill(W, n));
   int c = n / 2;
   int lo = c - num_injection_cells, hi = c + num_injection_cells;
   // a Python slice with negative start counts from the end; the reference's
   // callers use k = n // 16, so lo >= 0 there; reject the wrap-around case
   if (lo < 0) return set_error(TF_ERR_ARG, "num_injection_cells larger than n/2");
   if (hi > n) hi = n;
-  long long n3 = (long long)n * n * n;
-  ics_cube_kernel<<<ics_grid(n3), 256, 0, (cudaStream_t)stream>>>(W, n, lo, hi);
+  ics_cube_kernel<<<fill_grid(n), fill_threads(n), 0, (cudaStream_t)stream>>>(W, n, lo, hi);
   return launch_check("ics_cube_kernel");
 }
 
@@ -112,10 +134,9 @@ int tf_ics_injection_cube(float* W, int n, int num_injection_cells, void* stream
 // rho = rho0 * (1 + noise * U(-1, 1)) from the seeded hash.
 int tf_ics_overpressure(float* W, int n, unsigned long long seed, double radius, double p_in,
                         double p_out, double rho0, double noise, void* stream) {
-  if (!W || n < 1) return set_error(TF_ERR_ARG, "bad arguments");
-  long long n3 = (long long)n * n * n;
-  ics_overpressure_kernel<<<ics_grid(n3), 256, 0, (cudaStream_t)stream>>>(W, n, seed, radius, p_in,
-                                                                          p_out, rho0, noise);
+  TF_TRY(check_fill(W, n));
+  ics_overpressure_kernel<<<fill_grid(n), fill_threads(n), 0, (cudaStream_t)stream>>>(
+      W, n, seed, (float)radius, (float)p_in, (float)p_out, (float)rho0, (float)noise);
   return launch_check("ics_overpressure_kernel");
 }
 
@@ -123,9 +144,9 @@ int tf_ics_overpressure(float* W, int n, unsigned long long seed, double radius,
 // vx = -0.5; p = 2.5; vy = amplitude * sin(4 pi x) * a, a ~ N(0, 1) per cell
 // from the seeded hash; vz = 0.
 int tf_ics_shear_layer(float* W, int n, unsigned long long seed, double amplitude, void* stream) {
-  if (!W || n < 1) return set_error(TF_ERR_ARG, "bad arguments");
-  long long n3 = (long long)n * n * n;
-  ics_shear_kernel<<<ics_grid(n3), 256, 0, (cudaStream_t)stream>>>(W, n, seed, amplitude);
+  TF_TRY(check_fill(W, n));
+  ics_shear_kernel<<<fill_grid(n), fill_threads(n), 0, (cudaStream_t)stream>>>(W, n, seed,
+                                                                             (float)amplitude);
   return launch_check("ics_shear_kernel");
 }
 
