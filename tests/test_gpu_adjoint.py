@@ -31,7 +31,7 @@ def grad_of(loss_fn, U0):
     U = U0.clone().requires_grad_(True)
     loss = loss_fn(U)
     loss.backward()
-    return U.grad, float(loss)
+    return U.grad, float(loss.detach())
 
 
 def test_adjoint_matches_autograd_of_reference_restatement(tg):
