@@ -101,6 +101,27 @@ int tf_evolve_state(const float *W_in, float *W_out, int nx, int ny, int nz, flo
                     float dt_host, const float *dt_dev, float gamma, unsigned flags,
                     const tf_tile_config *tile, void *stream);
 
+/* Diagnostics (the headless form of scaling_jax.py:75-82 plot_results, which
+ * shows rho and p on the plane z = n//2, plus conserved totals); no reference
+ * C counterpart.
+ *
+ * tf_evolve_state_diag: tf_evolve_state (same arguments and result, per-thread
+ * loads) that in the same pass writes totals[0..4] = sums over all cells of the
+ * NEW state's conserved variables (rho, rho vx, rho vy, rho vz, E per
+ * fluid.py:30-67; float32 per thread, float64 across threads; not multiplied
+ * by the cell volume) and, when slice is non-NULL, slice[0][x][y] = rho and
+ * slice[1][x][y] = p of the plane z = z_slice (2*nx*ny floats).  totals (5
+ * device doubles) is zeroed by the call.
+ *
+ * tf_diagnostics: the same outputs for any stored primitive state in one
+ * read pass (float64 sums per thread). */
+int tf_evolve_state_diag(const float *W_in, float *W_out, int nx, int ny, int nz, float dx,
+                         float dt_host, const float *dt_dev, float gamma, unsigned flags,
+                         const tf_tile_config *tile, double *totals, float *slice, int z_slice,
+                         void *stream);
+int tf_diagnostics(const float *W, int nx, int ny, int nz, float gamma, double *totals,
+                   float *slice, int z_slice, void *stream);
+
 /* time_integration.py:94-128 (plain branch): while t < t_final: dt = CFL dt;
  * W = step(W, dt); t += dt; iter += 1.  max_steps >= 0 also bounds the loop
  * (0 = t_final only is NOT implied: pass -1 for unbounded).  fixed_dt > 0

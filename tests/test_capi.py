@@ -72,6 +72,12 @@ def test_host_side_argument_checks(lib):
         tc = _lib.TileConfig(34, 4, 0)  # not one of 8, 16, 32
         _lib.call("tf_evolve_state", fake, other, 4, 4, 4, 0.1, 0.01, None, 5 / 3, 0,
                   ctypes.byref(tc), None)
+    third = ctypes.c_void_p(0x3000)
+    with pytest.raises(_lib.TinyfluidsError):  # slice plane outside the grid
+        _lib.call("tf_evolve_state_diag", fake, other, 4, 4, 4, 0.1, 0.01, None, 5 / 3, 0, None,
+                  third, third, 4, None)
+    with pytest.raises(_lib.TinyfluidsError):  # diagnostics need a totals buffer
+        _lib.call("tf_diagnostics", fake, 4, 4, 4, 5 / 3, None, None, 0, None)
     with pytest.raises(_lib.TinyfluidsError):  # unbounded loop
         _lib.call("tf_time_integration", fake, other, ctypes.c_void_p(0x3000),
                   ctypes.c_void_p(0x4000), 4, 4, 4, 0.1, float("inf"), 5 / 3, 0.4, -1, 0.0, 0,

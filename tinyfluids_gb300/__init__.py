@@ -6,7 +6,7 @@ A drop-in for the reference's hot path, ``tinyfluids.jax_tinyfluids``:
 float32 layout, on CUDA tensors.  All compute runs in the hand-written kernels
 of ``csrc/`` behind the C ABI in ``include/tinyfluids_gb300.h``.
 """
-from . import fluid, time_integration, initial_conditions  # noqa: F401
+from . import fluid, time_integration, initial_conditions, diagnostics  # noqa: F401
 from .fluid import (DENSITY_INDEX, PRESSURE_INDEX, VAR_AXIS, VELOCITY_X_INDEX,  # noqa: F401
                     VELOCITY_Y_INDEX, VELOCITY_Z_INDEX, X_AXIS, Y_AXIS, Z_AXIS,
                     _cfl_time_step, _euler_flux, _evolve_state, _evolve_state_along_axis,

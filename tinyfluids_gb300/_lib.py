@@ -55,6 +55,9 @@ SIGNATURES = {
     "tf_cfl_time_step": (c_int, [vp, c_int, c_int, c_int, c_float, c_float, c_float, vp, vp]),
     "tf_evolve_state": (c_int, [vp, vp, c_int, c_int, c_int, c_float, c_float, vp, c_float,
                                 c_uint, vp, vp]),
+    "tf_evolve_state_diag": (c_int, [vp, vp, c_int, c_int, c_int, c_float, c_float, vp,
+                                     c_float, c_uint, vp, vp, vp, c_int, vp]),
+    "tf_diagnostics": (c_int, [vp, c_int, c_int, c_int, c_float, vp, vp, c_int, vp]),
     "tf_time_integration": (c_int, [vp, vp, vp, vp, c_int, c_int, c_int, c_float, c_float,
                                     c_float, c_float, c_int, c_float, c_uint, vp, vp, vp]),
     "tf_evolve_along_axis": (c_int, [vp, vp, c_int, c_int, c_int, c_float, c_float, vp,

@@ -53,6 +53,48 @@ __device__ __forceinline__ float block_max(float v, float* red) {
   return __uint_as_float(b);
 }
 
+// Compensated float32 sum (Knuth's TwoSum): s + c carries the running sum
+// to about twice float32 precision, so per-thread partials need no float64
+// arithmetic (a small fraction of the float32 rate on this GPU).  The
+// operations must not be reassociated: they contain no products, so no FMA
+// contraction applies either.
+struct CSum {
+  float s, c;
+};
+__device__ __forceinline__ void csum_add(CSum& a, float x) {
+  const float t = a.s + x;
+  const float z = t - a.s;
+  a.c += (a.s - (t - z)) + (x - z);
+  a.s = t;
+}
+
+// Sums five per-thread partials over the block in float64 and adds them to
+// totals[0..4] (one atomic per component per CTA).  `red` needs 5 doubles per
+// warp.  Every thread of the block must call it.
+__device__ __forceinline__ void block_add_totals(const CSum acc[5], double* red,
+                                                 double* totals) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  double v[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    v[i] = (double)acc[i].s + (double)acc[i].c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+  }
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) red[w * 5 + i] = v[i];
+  }
+  __syncthreads();
+  if (threadIdx.x < 5) {
+    double sum = 0.0;
+    for (int k = 0; k < nw; ++k) sum += red[k * 5 + threadIdx.x];
+    atomicAdd(totals + threadIdx.x, sum);
+  }
+}
+
 // Volatile reads of control fields written by other kernels/CTAs.
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
 __device__ __forceinline__ float ld_volatile(const float* p) { return *(const volatile float*)p; }

@@ -77,7 +77,37 @@ struct TileOut {
   size_t plane, vstride, dcol_a, dcol_b;
   bool store_a, store_b;
   float wmax;
+  // diagnostics (set only by the diagnostics instantiation)
+  CSum acc[5];         // running sums of the stored cells' conserved variables
+  float* slice;        // [2][nx][ny]: rho and p of the plane z == z_slice, or null
+  size_t slice_plane;  // nx * ny
+  int ny, sy_a, sy_b;  // y of cell a / b if it lies on the slice plane, else -1
 };
+
+// Diagnostics output of a fused step: conserved totals and, optionally, the
+// density and pressure of one z plane (the reference's plot_results slice,
+// scaling_jax.py:75-82).
+struct DiagArgs {
+  float* slice;
+  int z_slice;
+};
+
+// Conserved variables of one stored primitive cell (the reference's
+// conversion, fluid.py:30-67) into the running totals, and its slice values.
+__device__ __forceinline__ void diag_cell(TileOut& o, int x, int sy, const V2 wo[5], bool hi,
+                                          const StepConsts<float>& K) {
+  float w[5], u[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) w[i] = hi ? wo[i].y : wo[i].x;
+  exact_cons_from_prim(w, u, K);
+#pragma unroll
+  for (int i = 0; i < 5; ++i) csum_add(o.acc[i], u[i]);
+  if (sy >= 0) {
+    const size_t j = (size_t)x * o.ny + sy;
+    o.slice[j] = w[0];
+    o.slice[o.slice_plane + j] = w[4];
+  }
+}
 
 __device__ __forceinline__ void store5(const TileOut& o, int x, size_t dcol, const V2 wo[5],
                                        bool hi) {
@@ -93,7 +123,7 @@ __device__ __forceinline__ void store5(const TileOut& o, int x, size_t dcol, con
 // `after_sync()` runs after the plane's first CTA barrier, when every thread
 // has read plane x+1 (the TMA loader refills its stage there) and returns
 // true if the CTA must stop (a bounded wait gave up).
-template <class P, int NWP, class Consumed, class AfterSync>
+template <class P, int NWP, bool DIAG = false, class Consumed, class AfterSync>
 __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, const V2 fm[5],
                                              Cell2& nxt, V2 fp[5], const StepConsts<float>& K,
                                              FusedSmem<NWP>& sm, TileOut& o, Consumed consumed,
@@ -183,10 +213,12 @@ __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, 
   if (o.store_a) {
     store5(o, x, o.dcol_a, wo, false);
     o.wmax = speed_max(o.wmax, sp.x);
+    if constexpr (DIAG) diag_cell(o, x, o.sy_a, wo, false, K);
   }
   if (o.store_b) {
     store5(o, x, o.dcol_b, wo, true);
     o.wmax = speed_max(o.wmax, sp.y);
+    if constexpr (DIAG) diag_cell(o, x, o.sy_b, wo, true, K);
   }
   return stop;
 }
@@ -231,12 +263,26 @@ __device__ __forceinline__ TileCols tile_cols(const FusedGeom& G, int tz, int ty
 // L2-only loads (ld.global.cg) for kernels that read data other CTAs wrote
 // earlier in the same launch (the persistent batch kernel); otherwise loads
 // use the read-only path.
-template <class P, int NWP, bool COHERENT = false>
+// DIAG: also accumulate the stored cells' conserved totals into acc[5] and
+// write the slice of `d` (the diagnostics instantiation of the single step).
+template <class P, int NWP, bool COHERENT = false, bool DIAG = false>
 __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float* __restrict__ dst,
                                             const FusedGeom& G, int tz, int ty, int tx,
-                                            const StepConsts<float>& K, FusedSmem<NWP>& sm) {
+                                            const StepConsts<float>& K, FusedSmem<NWP>& sm,
+                                            DiagArgs d = DiagArgs{nullptr, -1},
+                                            CSum* acc = nullptr) {
   TileOut o;
   const TileCols t = tile_cols<NWP>(G, tz, ty, tx, src, dst, o);
+  if constexpr (DIAG) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) o.acc[i] = CSum{0.f, 0.f};
+    o.slice = d.slice;
+    o.slice_plane = (size_t)G.nx * G.ny;
+    o.ny = G.ny;
+    const bool on = d.slice != nullptr && t.z == d.z_slice;
+    o.sy_a = on && o.store_a ? t.ya : -1;
+    o.sy_b = on && o.store_b ? t.yb : -1;
+  }
   const bool open = G.open_bc != 0;
   auto ld = [&](const float* p) { return COHERENT ? __ldcg(p) : __ldg(p); };
   auto load = [&](int x, V2 v[5]) {
@@ -272,18 +318,22 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
   // Two planes per trip so the prefetch buffers alternate without moves;
   // `pf` holds plane x+1 on entry and receives plane x+3.
   for (int x = t.x0; x < t.x_end; x += 2) {
-    plane_update<P, NWP>(x, pb, c0, f0, c1, f1, K, sm, o,
+    plane_update<P, NWP, DIAG>(x, pb, c0, f0, c1, f1, K, sm, o,
                          [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); }, sync_only);
     c0 = c1;
 #pragma unroll
     for (int i = 0; i < 5; ++i) f0[i] = f1[i];
     if (x + 1 < t.x_end) {
-      plane_update<P, NWP>(x + 1, pa, c0, f0, c1, f1, K, sm, o,
+      plane_update<P, NWP, DIAG>(x + 1, pa, c0, f0, c1, f1, K, sm, o,
                            [&]() { if (x + 4 <= t.x_end) load(x + 4, pa); }, sync_only);
       c0 = c1;
 #pragma unroll
       for (int i = 0; i < 5; ++i) f0[i] = f1[i];
     }
+  }
+  if constexpr (DIAG) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) acc[i] = o.acc[i];
   }
   return o.wmax;
 }

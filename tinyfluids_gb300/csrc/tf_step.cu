@@ -148,6 +148,39 @@ __global__ void final_select_kernel(const tf_ctl* ctl, const float* __restrict__
   }
 }
 
+// Diagnostics of a stored primitive state in one pass: sums of the conserved
+// variables (fluid.py:30-67 per cell; compensated float32 per thread, float64
+// across threads) and the rho / p plane z == z_slice ([2][nx][ny], skipped
+// when slice is null).  Blocks stride over (x, y) rows, threads along z, so no
+// cell index is divided.
+__global__ void __launch_bounds__(256) diagnostics_kernel(const float* __restrict__ W, int nx,
+                                                          int ny, int nz, StepConsts<float> k,
+                                                          double* totals, float* slice,
+                                                          int z_slice) {
+  __shared__ double red[8 * 5];
+  const long long n = (long long)nx * ny * nz;
+  const long long rows = (long long)nx * ny;
+  CSum acc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) acc[v] = CSum{0.f, 0.f};
+  for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+    const float* row = W + r * nz;
+    for (int z = threadIdx.x; z < nz; z += blockDim.x) {
+      float w[5], u[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) w[v] = __ldg(row + v * n + z);
+      exact_cons_from_prim(w, u, k);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) csum_add(acc[v], u[v]);
+      if (slice && z == z_slice) {
+        slice[r] = w[0];
+        slice[rows + r] = w[4];
+      }
+    }
+  }
+  block_add_totals(acc, red, totals);
+}
+
 // ---------------------------------------------------------------------------
 // fused step
 // ---------------------------------------------------------------------------
@@ -161,11 +194,14 @@ struct FusedArgs {
   float fixed_dt;  // loop mode: > 0 replaces ctl->dt
   tf_ctl* ctl;     // fixed mode: optional; loop mode: required
   int loop;        // 1: predicated loop step (parity buffers, dt from ctl)
+  double* totals;  // diagnostics instantiation: conserved totals (zeroed before)
+  DiagArgs diag;   // diagnostics instantiation: optional slice
 };
 
-template <class P, int NWP>
+template <class P, int NWP, bool DIAG = false>
 __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_kernel(FusedArgs a) {
   __shared__ FusedSmem<NWP> sm;
+  __shared__ double dred[DIAG ? NWP * 5 : 1];
   const float* src;
   float* dst;
   float dt;
@@ -187,7 +223,10 @@ __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_ker
   K.inv_dx = a.inv_dx;
   K.dt = dt;
   K.k = dt * a.inv_dx;
-  float m = fused_tile<P, NWP>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z, K, sm);
+  CSum acc[5];
+  float m = fused_tile<P, NWP, false, DIAG>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z,
+                                            K, sm, a.diag, acc);
+  if constexpr (DIAG) block_add_totals(acc, dred, a.totals);
   if (a.ctl) {
     float bm = block_max(m, sm.red);
     if (threadIdx.x == 0)
@@ -380,7 +419,13 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
       return launch_check("fused_step_tma_kernel");
     }
   }
-  // 32-bit element offsets when the state has fewer than 2^31 floats
+  if (a.totals) {
+    TF_DISPATCH_ROWS(rows, NWP, {
+      if (exact) fused_step_kernel<ExactPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
+      else fused_step_kernel<FastPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
+    });
+    return launch_check("fused_step_kernel (diagnostics)");
+  }
   TF_DISPATCH_ROWS(rows, NWP, {
     if (exact) fused_step_kernel<ExactPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
     else fused_step_kernel<FastPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
@@ -533,6 +578,51 @@ int tf_evolve_state(const float* W_in, float* W_out, int nx, int ny, int nz, flo
   a.loop = 0;
   a.ctl = nullptr;
   return launch_fused(a, rows, (flags & TF_FLAG_EXACT) != 0, (cudaStream_t)stream, loader);
+}
+
+int tf_evolve_state_diag(const float* W_in, float* W_out, int nx, int ny, int nz, float dx,
+                         float dt_host, const float* dt_dev, float gamma, unsigned flags,
+                         const tf_tile_config* tile, double* totals, float* slice, int z_slice,
+                         void* stream) {
+  if (!W_in || !W_out || !totals) return set_error(TF_ERR_ARG, "null pointer");
+  if (W_in == W_out) return set_error(TF_ERR_ARG, "W_out must not alias W_in");
+  TF_TRY(check_dims(nx, ny, nz, flags));
+  TF_TRY(check_scalars(dx, gamma));
+  if (!dt_dev && !isfinite(dt_host)) return set_error(TF_ERR_ARG, "dt must be finite");
+  if (slice && (z_slice < 0 || z_slice >= nz))
+    return set_error(TF_ERR_ARG, "z_slice %d outside [0, %d)", z_slice, nz);
+  int rows, lx, loader;
+  TF_TRY(resolve_tile(tile, &rows, &lx, &loader));
+  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
+  FusedArgs a = make_fused_args(W_in, nullptr, W_out, geo, dx, gamma);
+  a.dt_host = dt_host;
+  a.dt_dev = dt_dev;
+  a.loop = 0;
+  a.ctl = nullptr;
+  a.totals = totals;
+  a.diag.slice = slice;
+  a.diag.z_slice = slice ? z_slice : -1;
+  cudaStream_t s = (cudaStream_t)stream;
+  TF_TRY(cuda_check(cudaMemsetAsync(totals, 0, 5 * sizeof(double), s), "cudaMemsetAsync"));
+  return launch_fused(a, rows, (flags & TF_FLAG_EXACT) != 0, s, 1);
+}
+
+int tf_diagnostics(const float* W, int nx, int ny, int nz, float gamma, double* totals,
+                   float* slice, int z_slice, void* stream) {
+  if (!W || !totals) return set_error(TF_ERR_ARG, "null pointer");
+  TF_TRY(check_dims(nx, ny, nz, 0));
+  TF_TRY(check_scalars(1.f, gamma));
+  if (slice && (z_slice < 0 || z_slice >= nz))
+    return set_error(TF_ERR_ARG, "z_slice %d outside [0, %d)", z_slice, nz);
+  cudaStream_t s = (cudaStream_t)stream;
+  TF_TRY(cuda_check(cudaMemsetAsync(totals, 0, 5 * sizeof(double), s), "cudaMemsetAsync"));
+  const long long rows = (long long)nx * ny;
+  const long long cap = (long long)sm_count() * 8;
+  const int threads = nz >= 256 ? 256 : ((nz + 31) / 32) * 32;
+  diagnostics_kernel<<<(int)(rows < cap ? rows : cap), threads, 0, s>>>(W, nx, ny, nz,
+                                                         make_consts<float>(gamma, 1.f, 0.f),
+                                                         totals, slice, z_slice);
+  return launch_check("diagnostics_kernel");
 }
 
 int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ctl, int nx, int ny,
