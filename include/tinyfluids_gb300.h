@@ -44,6 +44,9 @@ typedef enum tf_status {
 #define TF_FLAG_EXACT 2u           /* reference op order, bit-identical to the oracle */
 #define TF_FLAG_IN_CONSERVED 4u    /* tf_evolve_along_axis, fast policy: input is conserved */
 #define TF_FLAG_OUT_CONSERVED 8u   /* tf_evolve_along_axis, fast policy: output is conserved */
+#define TF_FLAG_HOST_LOOP 16u      /* tf_time_integration, t_final loop: test the condition on
+                                      the host once per chunk of steps instead of in a CUDA
+                                      graph's device-side while node */
 
 /*
  * Device-resident control block of a run (64 bytes, caller-allocated device
@@ -67,8 +70,9 @@ typedef struct tf_ctl {
   int reserved[5];
 } tf_ctl;
 
-/* Tile shape of the fused step kernel; NULL = built-in heuristic (16 rows,
- * lx for about eight waves of resident CTAs). */
+/* Tile shape of the fused step kernel; NULL = built-in heuristic (16 rows;
+ * lx for about nine waves of resident CTAs in chunks of >= 16 planes, shorter
+ * chunks for grids that would not fill one wave). */
 typedef struct tf_tile_config {
   int rows;    /* grid rows per tile incl. the 1-cell ring: 8, 16 or 32 (rows/2 warps) */
   int lx;      /* x planes per CTA (>= 1; 0 = heuristic) */
@@ -128,9 +132,14 @@ int tf_diagnostics(const float *W, int nx, int ny, int nz, float gamma, double *
  * replaces the CFL dt (the fixed-dt form used for differentiation).
  * work: scratch state of the same size (ping-pong).  The final state is in
  * W_out; ctl holds t, iter and status.  If iters_host is non-NULL the call
- * blocks until the loop ends and stores the iteration count there; the
- * t_final loop always synchronises once per chunk of steps to test the
- * condition. */
+ * blocks until the loop ends and stores the iteration count there.
+ * A known step count (max_steps >= 0) enqueues that many predicated steps.
+ * A t_final loop (max_steps < 0) runs as one CUDA graph whose while node
+ * repeats {step, condition} on the device until the loop condition fails, a
+ * step no longer advances float32 t (TF_ERR_NONFINITE: the reference would
+ * loop forever) or 2^24 conditions have been evaluated (TF_ERR_TIMEOUT):
+ * nothing waits on the host.  TF_FLAG_HOST_LOOP instead tests the condition
+ * on the host once per chunk of steps. */
 int tf_time_integration(const float *W_in, float *W_out, float *work, tf_ctl *ctl, int nx,
                         int ny, int nz, float dx, float t_final, float gamma, float cfl,
                         int max_steps, float fixed_dt, unsigned flags,

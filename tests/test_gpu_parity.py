@@ -99,10 +99,13 @@ def test_dt_from_device_tensor(tg):
 
 
 @pytest.mark.parametrize("n", [32, 64, 96, 128, 196, 256])
-def test_exact_time_integration_reproduces_reference_counts(tg, oracle_lib, n):
-    """The reference's golden data: steps to t=0.2 for setup_ics(n, n//16)."""
+@pytest.mark.parametrize("host_loop", [False, True])
+def test_exact_time_integration_reproduces_reference_counts(tg, oracle_lib, n, host_loop):
+    """The reference's golden data: steps to t=0.2 for setup_ics(n, n//16),
+    with the loop as a device-side graph while node and as host-checked chunks."""
     W, dx = tg.setup_ics(n, n // 16)
-    Wf, it = tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False, exact=True)
+    Wf, it = tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False, exact=True,
+                                    host_loop=host_loop)
     assert int(it) == GOLDEN["counts"][str(n)]
     if n <= 64:
         ref, rit = oracle_lib.time_integration(host(W), dx, 0.2, GAMMA, True)
@@ -115,6 +118,19 @@ def test_fast_time_integration_reproduces_reference_counts(tg, n):
     W, dx = tg.setup_ics(n, n // 16)
     _, it = tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False)
     assert int(it) == GOLDEN["counts"][str(n)]
+
+
+@pytest.mark.parametrize("shape,t_final", [((48, 48, 48), 0.05), ((33, 17, 61), 0.02),
+                                           ((1, 1, 1), 0.3)])
+def test_graph_loop_matches_host_loop(tg, shape, t_final):
+    W = dev(random_state(shape, 8))
+    a, ia = tg.time_integration_fn(W, 0.05, t_final, GAMMA, False, False)
+    b, ib = tg.time_integration_fn(W, 0.05, t_final, GAMMA, False, False, host_loop=True)
+    assert int(ia) == int(ib) > 0
+    assert torch.equal(a, b)
+    # repeated calls build a fresh graph each time and give the same result
+    c, ic = tg.time_integration_fn(W, 0.05, t_final, GAMMA, False, False)
+    assert int(ic) == int(ia) and torch.equal(c, a)
 
 
 def test_setup_ics_matches_reference_builder(tg):
@@ -194,11 +210,12 @@ def test_overpressure_64_accuracy_vs_fp64(tg, oracle_lib):
     assert e_fast_l1 <= 2 * e_ref_l1 and e_fast_inf <= 2 * e_ref_inf
 
 
-def test_nonfinite_state_is_reported(tg):
+@pytest.mark.parametrize("host_loop", [False, True])
+def test_nonfinite_state_is_reported(tg, host_loop):
     W = random_state((8, 8, 8), 1)
     W[4, 3, 3, 3] = -1.0  # negative pressure: sound speed is NaN
     with pytest.raises(tg.TinyfluidsError) as e:
-        tg.time_integration_fn(dev(W), 0.1, 0.5, GAMMA, False, False)
+        tg.time_integration_fn(dev(W), 0.1, 0.5, GAMMA, False, False, host_loop=host_loop)
     assert e.value.status == 3
 
 

@@ -92,6 +92,7 @@ TF_FLAG_OPEN_BOUNDARIES = 1
 TF_FLAG_EXACT = 2
 TF_FLAG_IN_CONSERVED = 4
 TF_FLAG_OUT_CONSERVED = 8
+TF_FLAG_HOST_LOOP = 16
 
 
 class TinyfluidsError(RuntimeError):

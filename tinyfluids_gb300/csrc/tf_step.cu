@@ -105,6 +105,35 @@ __global__ void ctl_init_kernel(tf_ctl* ctl, float t_final, float cfl_dx, int ma
   ctl->max_steps = max_steps;
   ctl->status = TF_OK;
   ctl->max_speed = 0.f;
+  for (int i = 0; i < 5; ++i) ctl->reserved[i] = 0;
+}
+
+// Condition of the device-side t_final loop (a CUDA graph while node): the
+// loop condition the last step left in ctl->active, stopped early when
+// float32 t did not advance since the previous evaluation (a stalled loop
+// the reference would never leave) or after `cap` evaluations.  Every body
+// iteration runs this kernel once, so the evaluation count bounds the loop
+// whatever the step kernel does.  ctl->reserved[0] counts evaluations,
+// reserved[1] holds the bits of t at the previous one.
+constexpr int kGraphLoopCap = 1 << 24;
+
+__global__ void loop_cond_kernel(tf_ctl* ctl, cudaGraphConditionalHandle h, int cap) {
+  const int evals = ctl->reserved[0] + 1;
+  const float t = ld_volatile(&ctl->t);
+  const float t_prev = __int_as_float(ctl->reserved[1]);
+  int active = ld_volatile(&ctl->active);
+  if (active && evals > 1 && t == t_prev) {
+    ctl->status = TF_ERR_NONFINITE;
+    active = 0;
+  }
+  if (active && evals > cap) {
+    ctl->status = TF_ERR_TIMEOUT;
+    active = 0;
+  }
+  ctl->active = active;
+  ctl->reserved[0] = evals;
+  ctl->reserved[1] = __float_as_int(t);
+  cudaGraphSetConditional(h, active ? 1u : 0u);
 }
 
 // Max wave speed of a primitive state (fluid.py:427-500 in per-cell form);
@@ -353,12 +382,26 @@ static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int
   g.tiles_z = (nz + kTileZ - 1) / kTileZ;
   g.tiles_y = (ny + (rows - 2) - 1) / (rows - 2);
   if (lx <= 0) {
-    // enough CTAs for ~12 waves of resident CTAs, chunks of >= 8 planes
-    // (512^3, 16-row tiles: 6 chunks of 86 planes)
-    long long tiles_yz = (long long)g.tiles_z * g.tiles_y;
-    long long want = 12LL * sm_count() * min_ctas_per_sm(rows / 2);
-    long long tx = (want + tiles_yz - 1) / tiles_yz;
-    long long max_tx = nx / 8 > 0 ? nx / 8 : 1;
+    // About 9 waves of resident CTAs, in chunks of >= 16 planes (each chunk
+    // re-reads one plane and warms up its carry); grids too small for one
+    // wave at that chunk length take 8-plane chunks, and grids too small for
+    // one wave even then are latency-bound and take the chunk length that
+    // makes one wave, but at least 2 planes.  Measured on GB300 with the
+    // reference's benchmark states: 32^3 -> 2 planes, 64^3 -> 4, 96^3 -> 8,
+    // 128^3 and 256^3 -> 16, 512^3 -> 103 (5 chunks).
+    const long long tiles_yz = (long long)g.tiles_z * g.tiles_y;
+    const long long resident = (long long)sm_count() * min_ctas_per_sm(rows / 2);
+    long long min_planes;
+    if (tiles_yz * (nx / 16) >= resident) {
+      min_planes = 16;
+    } else if (tiles_yz * (nx / 8) >= resident) {
+      min_planes = 8;
+    } else {
+      min_planes = (nx * tiles_yz + resident - 1) / resident;
+      if (min_planes < 2) min_planes = 2;
+    }
+    long long tx = (9 * resident + tiles_yz - 1) / tiles_yz;
+    long long max_tx = nx / min_planes > 0 ? nx / min_planes : 1;
     if (tx > max_tx) tx = max_tx;
     if (tx < 1) tx = 1;
     lx = (int)((nx + tx - 1) / tx);
@@ -431,6 +474,123 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
     else fused_step_kernel<FastPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
   });
   return launch_check("fused_step_kernel");
+}
+
+// The t_final loop as a CUDA graph: a while node whose body is {one
+// predicated fused step, loop_cond_kernel}, entered after one condition
+// evaluation.  The kernel arguments bake in the buffers and scalars, so
+// executable graphs are cached by (device, arguments, tile): a repeated call
+// on the same buffers launches the cached graph.  An evicted graph is
+// destroyed at once; CUDA frees it after any in-flight launch completes.
+struct GraphKey {
+  int device, rows, exact;
+  FusedArgs a;  // zero-initialised, so padding compares equal
+};
+struct GraphEntry {
+  GraphKey key;
+  cudaGraphExec_t exec;
+};
+static std::mutex g_graph_mu;
+static std::vector<GraphEntry> g_graphs;  // most recently used last
+constexpr size_t kGraphCacheSize = 8;
+
+static int build_graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl,
+                            cudaGraphExec_t* out);
+
+static int graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, cudaStream_t s) {
+  GraphKey k;
+  memset(&k, 0, sizeof k);
+  TF_TRY(cuda_check(cudaGetDevice(&k.device), "cudaGetDevice"));
+  k.rows = rows;
+  k.exact = exact ? 1 : 0;
+  k.a = a;
+  std::lock_guard<std::mutex> lk(g_graph_mu);
+  for (size_t i = 0; i < g_graphs.size(); ++i) {
+    if (memcmp(&g_graphs[i].key, &k, sizeof k) == 0) {
+      GraphEntry e = g_graphs[i];
+      g_graphs.erase(g_graphs.begin() + i);
+      g_graphs.push_back(e);
+      return cuda_check(cudaGraphLaunch(e.exec, s), "cudaGraphLaunch");
+    }
+  }
+  cudaGraphExec_t exec = nullptr;
+  TF_TRY(build_graph_loop(a, rows, exact, ctl, &exec));
+  int st = cuda_check(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
+  if (st != TF_OK) {
+    cudaGraphExecDestroy(exec);
+    return st;
+  }
+  if (g_graphs.size() >= kGraphCacheSize) {
+    cudaGraphExecDestroy(g_graphs.front().exec);
+    g_graphs.erase(g_graphs.begin());
+  }
+  g_graphs.push_back(GraphEntry{k, exec});
+  return TF_OK;
+}
+
+static int build_graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl,
+                            cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr, body = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cs = nullptr;
+  int st = TF_OK;
+  auto fail = [&](cudaError_t e, const char* what) {
+    if (st == TF_OK && e != cudaSuccess) st = cuda_check(e, what);
+    return st != TF_OK;
+  };
+  do {
+    if (fail(cudaGraphCreate(&g, 0), "cudaGraphCreate")) break;
+    cudaGraphConditionalHandle h;
+    if (fail(cudaGraphConditionalHandleCreate(&h, g, 0, 0), "cudaGraphConditionalHandleCreate"))
+      break;
+    // entry: evaluate the condition once (t_final may already be reached)
+    cudaGraphNode_t entry;
+    cudaKernelNodeParams kp;
+    memset(&kp, 0, sizeof kp);
+    int cap = kGraphLoopCap;
+    void* cargs[3] = {(void*)&ctl, (void*)&h, (void*)&cap};
+    kp.func = (void*)loop_cond_kernel;
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(1);
+    kp.kernelParams = cargs;
+    if (fail(cudaGraphAddKernelNode(&entry, g, nullptr, 0, &kp), "cudaGraphAddKernelNode"))
+      break;
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};  // other members zero
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t loop;
+    if (fail(cudaGraphAddNode(&loop, g, &entry, nullptr, 1, &np), "cudaGraphAddNode(while)"))
+      break;
+    body = np.conditional.phGraph_out[0];
+    // the body: capture a step and the condition into the while node's graph
+    if (fail(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate")) break;
+    if (fail(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal),
+             "cudaStreamBeginCaptureToGraph"))
+      break;
+    int lst = launch_fused(a, rows, exact, cs, 1);
+    if (lst == TF_OK) {
+      loop_cond_kernel<<<1, 1, 0, cs>>>(ctl, h, kGraphLoopCap);
+      lst = launch_check("loop_cond_kernel");
+    }
+    cudaGraph_t captured = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(cs, &captured);
+    if (lst != TF_OK) {
+      st = lst;
+      break;
+    }
+    if (fail(ce, "cudaStreamEndCapture")) break;
+    if (fail(cudaGraphInstantiate(&exec, g, 0), "cudaGraphInstantiate")) break;
+  } while (false);
+  if (cs) cudaStreamDestroy(cs);
+  if (g) cudaGraphDestroy(g);
+  if (st != TF_OK && exec) {
+    cudaGraphExecDestroy(exec);
+    exec = nullptr;
+  }
+  *out = exec;
+  return st;
 }
 
 static FusedArgs make_fused_args(const float* src, float* b0, float* b1, const FusedGeom& geo,
@@ -666,6 +826,8 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
   if (max_steps >= 0) {
     // step count known: enqueue exactly that many predicated steps
     for (int i = 0; i < max_steps; ++i) TF_TRY(launch_fused(a, rows, exact, s, loader));
+  } else if (!(flags & TF_FLAG_HOST_LOOP)) {
+    TF_TRY(graph_loop(a, rows, exact, ctl, s));
   } else {
     // run to t_final: chunks of predicated steps, one host check per chunk
     static thread_local tf_ctl* pinned = nullptr;

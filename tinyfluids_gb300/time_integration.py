@@ -4,9 +4,11 @@
 (time_integration.py:35-128): ``while t < t_final: dt = CFL dt(W);
 W = evolve(W, dt); t += dt; num_iterations += 1``, with ``t`` accumulated in
 float32 and the last step not clamped.  The loop runs on the device: each
-step is one fused kernel that also produces the next dt, and steps past the
-end are predicated off, so the host checks the condition only once per chunk
-of steps.
+step is one fused kernel that also produces the next dt and the loop
+condition, and the loop itself is a CUDA graph with a device-side while node
+(the counterpart of the reference's ``lax.while_loop``), so the host waits
+only for the result.  ``host_loop=True`` selects the older form that tests
+the condition on the host once per chunk of predicated steps.
 """
 from __future__ import annotations
 
@@ -21,7 +23,7 @@ from .fluid import (CTL_ITER, CTL_STATUS, CTL_T, _flags, _scalar, _stream, _tile
 
 def time_integration(primitive_state, grid_spacing, t_final, gamma, handle_boundaries,
                      shard_mapped, padding=None, split=None, *, C_CFL=0.4, exact=None,
-                     tile=None):
+                     tile=None, host_loop=False):
     """time_integration.py:94-128.  Returns ``(state, num_iterations)``;
     ``num_iterations`` is a 0-d int32 CUDA tensor like the reference's traced
     counter.  ``shard_mapped=True`` (the multi-GPU shard_map branch) is out of
@@ -31,7 +33,7 @@ def time_integration(primitive_state, grid_spacing, t_final, gamma, handle_bound
             "the shard_map branch (shard_mapped/padding/split) is not part of this "
             "single-GPU implementation")
     W, _, ctl = _run(primitive_state, grid_spacing, gamma, float(t_final), -1, 0.0,
-                     handle_boundaries, C_CFL, exact, tile, wait=True)
+                     handle_boundaries, C_CFL, exact, tile, wait=True, host_loop=host_loop)
     return W, ctl[CTL_ITER].clone()
 
 
@@ -51,7 +53,7 @@ def run_steps(primitive_state, grid_spacing, gamma, num_steps, handle_boundaries
 
 
 def _run(primitive_state, grid_spacing, gamma, t_final, max_steps, fixed_dt,
-         handle_boundaries, C_CFL, exact, tile, wait):
+         handle_boundaries, C_CFL, exact, tile, wait, host_loop=False):
     W = check_state(primitive_state)
     _, nx, ny, nz = W.shape
     with torch.cuda.device(W.device):
@@ -62,7 +64,9 @@ def _run(primitive_state, grid_spacing, gamma, t_final, max_steps, fixed_dt,
         _lib.call("tf_time_integration", W.data_ptr(), out.data_ptr(), work.data_ptr(),
                   ctl.data_ptr(), nx, ny, nz, float(grid_spacing), float(t_final),
                   _scalar(gamma, "gamma"), _scalar(C_CFL, "C_CFL"), int(max_steps),
-                  float(fixed_dt), _flags(handle_boundaries, exact), _tile_arg(tile, W, exact),
+                  float(fixed_dt),
+                  _flags(handle_boundaries, exact) | (_lib.TF_FLAG_HOST_LOOP if host_loop else 0),
+                  _tile_arg(tile, W, exact),
                   _lib.ctypes.byref(it) if wait else None, _stream(W))
     return out, (it.value if wait else None), ctl
 
