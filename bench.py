@@ -405,18 +405,22 @@ def run_serve_workload(args):
     from tinyfluids_gb300 import serving
     rates = [float(r) for r in args.rates.split(",")]
     sweep = []
+    def fresh(reqs):
+        return [serving.Request(r.rid, r.n, r.steps, r.ic, r.seed, r.arrival) for r in reqs]
+
     for rate in rates:
         reqs = serving.poisson_requests(args.requests, rate, seed=int(rate))
-        srv = serving.Server(hbm_budget=120e9, device=dev)
-        st = serving.latency_stats(srv.serve(reqs))
-        base = serving.serve_one_at_a_time(
-            [serving.Request(r.rid, r.n, r.steps, r.ic, r.seed, r.arrival) for r in reqs],
-            device=dev)
-        bt = serving.latency_stats(base)
-        sweep.append({"rate": rate, "served": st, "one_at_a_time": bt, "ticks": srv.ticks,
-                      "solves_per_s_ratio": st["solves_per_s"] / bt["solves_per_s"]})
+        srv = serving.Server(hbm_budget=120e9, device=dev, policy="srpt")
+        st = serving.latency_stats(srv.serve(fresh(reqs)))
+        srv_all = serving.Server(hbm_budget=120e9, device=dev, policy="all")
+        st_all = serving.latency_stats(srv_all.serve(fresh(reqs)))
+        bt = serving.latency_stats(serving.serve_one_at_a_time(fresh(reqs), device=dev))
+        sweep.append({"rate": rate, "served": st, "served_all_in_every_tick": st_all,
+                      "one_at_a_time": bt, "ticks": srv.ticks,
+                      "solves_per_s_ratio": st["solves_per_s"] / bt["solves_per_s"],
+                      "p50_ratio": bt["p50_s"] / st["p50_s"]})
     top = sweep[-1]
-    line = {"metric": "served solves/s, p50/p99 latency (continuous batching)",
+    line = {"metric": "served solves/s, p50/p99 latency (continuous batching, SRPT ticks)",
             "value": top["served"]["solves_per_s"], "unit": "solves/s", "higher_is_better": True,
             "n_gpus": 1, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{args.requests} requests per rate, N U[32,256], steps "

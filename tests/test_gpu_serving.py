@@ -15,11 +15,14 @@ def alone(tg, r):
     return tg.run_steps(W, dx, GAMMA, r.steps)
 
 
-def test_served_results_equal_alone(tg):
+@pytest.mark.parametrize("policy,tick_budget", [("all", 2 ** 27), ("srpt", 2 ** 27),
+                                                ("srpt", 60000), ("srpt", 1)])
+def test_served_results_equal_alone(tg, policy, tick_budget):
     reqs = [Request(0, 24, 13, "overpressure", 1, 0.0), Request(1, 40, 30, "shear", 2, 0.0),
             Request(2, 33, 7, "shear", 3, 0.0), Request(3, 17, 22, "overpressure", 4, 0.0),
             Request(4, 28, 1, "overpressure", 5, 0.0)]
-    srv = Server(hbm_budget=8e9, tick_steps=5, keep_states=True)
+    srv = Server(hbm_budget=8e9, tick_steps=5, keep_states=True, policy=policy,
+                 tick_budget=tick_budget)
     done = srv.serve(reqs)
     assert len(done) == len(reqs)
     for r in done:
@@ -57,6 +60,18 @@ def test_one_at_a_time_baseline_and_stats(tg):
     by_id = {r.rid: r for r in base}
     for r in done:  # same physics either way (mass is conserved and equal)
         assert r.result["mass"] == by_id[r.rid].result["mass"]
+
+
+def test_srpt_finishes_least_remaining_work_first(tg):
+    # a one-cell tick budget makes every tick hold exactly one request: the
+    # one with the least remaining work (cells x steps)
+    reqs = [Request(0, 40, 30, "shear", 2, 0.0), Request(1, 17, 3, "overpressure", 4, 0.0),
+            Request(2, 24, 9, "overpressure", 1, 0.0)]
+    srv = Server(hbm_budget=8e9, tick_steps=5, policy="srpt", tick_budget=1)
+    done = srv.serve(reqs)
+    assert [r.rid for r in done] == [1, 2, 0]
+    with pytest.raises(ValueError):
+        Server(policy="lifo")
 
 
 def test_oversized_request_rejected(tg):

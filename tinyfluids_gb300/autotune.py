@@ -66,9 +66,11 @@ def _key(device, shape, exact):
 
 
 def candidates(shape):
-    """(rows, lx) pairs worth timing for a grid shape."""
+    """(rows, lx) pairs worth timing for a grid shape; lx 0 is the built-in
+    chunk-length heuristic."""
     nx = shape[0]
-    lxs = sorted({lx for lx in (16, 32, 64, 96, 128, 192, 256, 512) if lx < nx} | {nx})
+    lxs = sorted({lx for lx in (2, 4, 8, 16, 32, 64, 96, 128, 192, 256, 512) if lx < nx}
+                 | {nx, 0})
     return [(r, lx) for r in ROWS for lx in lxs]
 
 
@@ -138,7 +140,7 @@ def size_class(n: int) -> int:
 
 
 def tune_batch(specs, exact=False, device=None, steps=2, candidates_rows=ROWS,
-               lx_policies=(0, 64, 32)):
+               lx_policies=(0, 64, 32, 16, 8)):
     """Tile choice for a batch: one `rows` for the launch and an `lx` per
     instance.  Inside a batch the GPU is full, so single-grid timings are a
     poor proxy; the candidates are timed on the batch itself (a short run of

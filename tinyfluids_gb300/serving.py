@@ -76,18 +76,33 @@ class _Active:
 
 
 class Server:
-    """Admits requests by free HBM budget and advances all admitted ones together.
+    """Admits requests by free HBM budget and advances admitted ones together.
 
-    A tick advances every active request by min(tick_steps, remaining) steps
-    in one persistent batch launch.  tick_steps is odd: a request's two
-    buffers alternate as input and output, and with the input doubling as
-    the work buffer an odd step count ends in the output buffer (no copy).
-    Batch plans are cached by the active set's buffers and step counts, which
-    recur every other tick while the set is stable, and at most two ticks are
-    in flight on the GPU."""
+    A tick advances a set of active requests by min(tick_steps, remaining)
+    steps each, in one persistent batch launch.  policy "all" puts every
+    active request in every tick (processor sharing).  policy "srpt" (the
+    default) takes active requests in order of least remaining work
+    (cells x remaining steps) until the tick holds `tick_budget`
+    cell-updates, so the GPU stays full while short requests finish first
+    instead of sharing the device with long ones; long requests run
+    whenever the short ones leave room.  tick_steps is odd: a request's two
+    buffers alternate as input and output, and with the input doubling as the
+    work buffer an odd step count ends in the output buffer (no copy).  Batch
+    plans are cached by the tick's buffers and step counts, which recur every
+    other tick while the set is stable, and at most two ticks are in flight
+    on the GPU."""
 
-    def __init__(self, hbm_budget=120e9, device=None, tick_steps=15, rows=16,
-                 cfl=0.4, keep_states=False, max_active=4096, plan_cache=4):
+    # defaults from a sweep on GB300 (60 Poisson requests, N U[32,256], steps
+    # U[50,500]): ticks of 31 steps and 2^29 cell-updates keep the throughput
+    # of putting every request in every tick while cutting the median latency
+    # about 5x
+    def __init__(self, hbm_budget=120e9, device=None, tick_steps=31, rows=16,
+                 cfl=0.4, keep_states=False, max_active=4096, plan_cache=4, policy="srpt",
+                 tick_budget=2 ** 29):
+        if policy not in ("srpt", "all"):
+            raise ValueError("policy must be 'srpt' or 'all'")
+        self.policy = policy
+        self.tick_budget = int(tick_budget)
         self.device = torch.device(device if device is not None else "cuda")
         self.budget = int(hbm_budget)
         self.tick_steps = int(tick_steps) | 1
@@ -125,14 +140,26 @@ class Server:
             req.admitted = now
 
     # -- one tick -----------------------------------------------------------
-    def _plan(self):
+    def _select(self):
+        """The requests of the next tick."""
+        if self.policy == "all" or len(self.active) <= 1:
+            return list(self.active)
+        chosen, work = [], 0
+        for a in sorted(self.active, key=lambda a: (a.req.n ** 3 * a.remaining, a.req.rid)):
+            chosen.append(a)
+            work += a.req.n ** 3 * min(self.tick_steps, a.remaining)
+            if work >= self.tick_budget:
+                break
+        return chosen
+
+    def _plan(self, group):
         key = tuple((a.cur.data_ptr(), a.other.data_ptr(), min(self.tick_steps, a.remaining))
-                    for a in self.active)
+                    for a in group)
         b = self._plans.pop(key, None)
         if b is None:
             specs = [InstanceSpec(a.cur, a.dx, a.req.gamma,
                                   num_steps=min(self.tick_steps, a.remaining), C_CFL=self.cfl,
-                                  out=a.other, consume_input=True) for a in self.active]
+                                  out=a.other, consume_input=True) for a in group]
             b = Batch(specs, rows=self.rows)
             while len(self._plans) >= self._plan_cache:
                 old = self._plans.pop(next(iter(self._plans)))
@@ -141,7 +168,8 @@ class Server:
         return b
 
     def _tick(self):
-        b = self._plan()
+        group = self._select()
+        b = self._plan(group)
         b.run()
         ev = torch.cuda.Event()
         ev.record(torch.cuda.current_stream(self.device))
@@ -149,7 +177,7 @@ class Server:
         while len(self._inflight) > 2:
             self._inflight.popleft().synchronize()
         self.ticks += 1
-        for a, sp in zip(self.active, b.specs):
+        for a, sp in zip(group, b.specs):
             a.cur, a.other = a.other, a.cur  # the result is in `out`
             a.remaining -= sp.num_steps
 
