@@ -51,7 +51,7 @@ __host__ __device__ constexpr int tile_rows_out(int nwp) { return 2 * nwp - 2; }
 
 template <int NWP>
 struct FusedSmem {
-  float4 cy[3][NWP][kTileLanes];  // lower cell of each thread's pair (U, F, u, c)
+  float4 cy[3][NWP][kTileLanes];  // lower cell of each thread's pair (U, F, wa, wb)
   float4 fy4[NWP][kTileLanes];    // face above each pair, components 0..3
   float fy1[NWP][kTileLanes];     // face above each pair, component 4
   float red[NWP];                 // block reduction
@@ -65,10 +65,10 @@ __device__ __forceinline__ void shfl_up_cell2(const Cell2& in, Cell2& out) {
     out.F[i].x = __shfl_up_sync(0xffffffffu, in.F[i].x, 1);
     out.F[i].y = __shfl_up_sync(0xffffffffu, in.F[i].y, 1);
   }
-  out.u.x = __shfl_up_sync(0xffffffffu, in.u.x, 1);
-  out.u.y = __shfl_up_sync(0xffffffffu, in.u.y, 1);
-  out.c.x = __shfl_up_sync(0xffffffffu, in.c.x, 1);
-  out.c.y = __shfl_up_sync(0xffffffffu, in.c.y, 1);
+  out.wa.x = __shfl_up_sync(0xffffffffu, in.wa.x, 1);
+  out.wa.y = __shfl_up_sync(0xffffffffu, in.wa.y, 1);
+  out.wb.x = __shfl_up_sync(0xffffffffu, in.wb.x, 1);
+  out.wb.y = __shfl_up_sync(0xffffffffu, in.wb.y, 1);
 }
 
 // Per-thread context of one tile: store targets and the running CFL speed.
@@ -145,7 +145,7 @@ __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, 
   P::template derive<2>(s1, cy, K);
   sm.cy[0][w][lane] = make_float4(cy.U[0].y, cy.U[1].y, cy.U[2].y, cy.U[3].y);
   sm.cy[1][w][lane] = make_float4(cy.U[4].y, cy.F[0].y, cy.F[1].y, cy.F[2].y);
-  sm.cy[2][w][lane] = make_float4(cy.F[3].y, cy.F[4].y, cy.u.y, cy.c.y);
+  sm.cy[2][w][lane] = make_float4(cy.F[3].y, cy.F[4].y, cy.wa.y, cy.wb.y);
   const bool stop = after_sync();
   // L = (cell above the pair, upper cell), R = (upper cell, lower cell):
   // faces (ya - 1/2, ya + 1/2).  Warp 0 has no cell above (its upper row
@@ -160,14 +160,14 @@ __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, 
     } else {
       a = make_float4(cy.U[0].x, cy.U[1].x, cy.U[2].x, cy.U[3].x);
       b = make_float4(cy.U[4].x, cy.F[0].x, cy.F[1].x, cy.F[2].x);
-      d = make_float4(cy.F[3].x, cy.F[4].x, cy.u.x, cy.c.x);
+      d = make_float4(cy.F[3].x, cy.F[4].x, cy.wa.x, cy.wb.x);
     }
     L.U[0] = v2(a.x, cy.U[0].x); L.U[1] = v2(a.y, cy.U[1].x);
     L.U[2] = v2(a.z, cy.U[2].x); L.U[3] = v2(a.w, cy.U[3].x);
     L.U[4] = v2(b.x, cy.U[4].x); L.F[0] = v2(b.y, cy.F[0].x);
     L.F[1] = v2(b.z, cy.F[1].x); L.F[2] = v2(b.w, cy.F[2].x);
     L.F[3] = v2(d.x, cy.F[3].x); L.F[4] = v2(d.y, cy.F[4].x);
-    L.u = v2(d.z, cy.u.x);       L.c = v2(d.w, cy.c.x);
+    L.wa = v2(d.z, cy.wa.x);     L.wb = v2(d.w, cy.wb.x);
   }
   V2 fy[5];
   P::hll(L, cy, fy);

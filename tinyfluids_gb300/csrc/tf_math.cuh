@@ -24,14 +24,18 @@
 namespace tf {
 
 // Quantities of one cell for a sweep along velocity index VEL (1, 2, 3):
-// conserved U, physical flux F along VEL, the normal velocity u and the
-// sound speed c (fluid.py:106-117, :208-259).
+// conserved U, physical flux F along VEL (fluid.py:208-259) and two wave
+// quantities that only the policy's own hll() reads: the exact policy keeps
+// the normal velocity u and the sound speed c (fluid.py:106-117), the fast
+// policies keep the wave-speed bounds u + c and c - u, which every face of
+// the cell needs and which are then computed once per cell instead of once
+// per face.
 template <typename T>
 struct Cell {
   T U[5];
   T F[5];
-  T u;
-  T c;
+  T wa;  // exact: u      fast: u + c
+  T wb;  // exact: c      fast: c - u
 };
 
 // ---------------------------------------------------------------------------
@@ -173,15 +177,15 @@ struct ExactPolicy {
     o.F[3] = O::mul(ud, O::mul(w[3], rho));
     o.F[4] = O::mul(ud, O::add(p, E));
     o.F[VEL] = O::add(o.F[VEL], p);
-    o.u = ud;
-    o.c = exact_sound(rho, p, k.g);
+    o.wa = ud;
+    o.wb = exact_sound(rho, p, k.g);
   }
 
   // fluid.py:282-303
   static __device__ __forceinline__ void hll(const Cell<T>& L, const Cell<T>& R, T F[5]) {
     using O = IEEE<T>;
-    T sp = O::mx(O::mx(O::add(L.u, L.c), O::add(R.u, R.c)), T(0));
-    T sm = O::mn(O::mn(O::sub(L.u, L.c), O::sub(R.u, R.c)), T(0));
+    T sp = O::mx(O::mx(O::add(L.wa, L.wb), O::add(R.wa, R.wb)), T(0));
+    T sm = O::mn(O::mn(O::sub(L.wa, L.wb), O::sub(R.wa, R.wb)), T(0));
     T smsp = O::mul(sm, sp);
     T den = O::sub(sp, sm);
 #pragma unroll
@@ -270,19 +274,23 @@ struct FastPolicy {
     o.F[3] = U[3] * ud;
     o.F[4] = (U[4] + p) * ud;
     o.F[VEL] = fmaf(U[VEL], ud, p);
-    o.u = ud;
-    o.c = sqrt_(k.g * p * ir);
+    const float c = sqrt_(k.g * p * ir);
+    o.wa = ud + c;
+    o.wb = c - ud;
   }
 
+  // HLL with ns = -S- = max(c_L - u_L, c_R - u_R, 0) (exactly the negated
+  // min of the reference's form): F = a F_L + b F_R + s (U_L - U_R) with
+  // a = S+/(S+ + ns), b = ns/(S+ + ns), s = ns a.
   static __device__ __forceinline__ void hll(const Cell<float>& L, const Cell<float>& R,
                                              float F[5]) {
-    float sp = fmaxf(fmaxf(L.u + L.c, R.u + R.c), 0.f);
-    float sm = fminf(fminf(L.u - L.c, R.u - R.c), 0.f);
-    float inv = rcp(sp - sm);
-    float a = sp * inv, b = sm * inv, s = sm * a;
+    float sp = fmaxf(fmaxf(L.wa, R.wa), 0.f);
+    float ns = fmaxf(fmaxf(L.wb, R.wb), 0.f);
+    float inv = rcp(sp + ns);
+    float a = sp * inv, b = ns * inv, s = ns * a;
 #pragma unroll
     for (int i = 0; i < 5; ++i)
-      F[i] = fmaf(a, L.F[i], fmaf(-b, R.F[i], s * (R.U[i] - L.U[i])));
+      F[i] = fmaf(a, L.F[i], fmaf(b, R.F[i], s * (L.U[i] - R.U[i])));
   }
 
   static __device__ __forceinline__ void update(const Cell<float>& C, const float flo[5],

@@ -18,11 +18,12 @@ namespace tf {
 
 typedef float2 V2;
 
+// Cell<float> of two cells (see Cell in tf_math.cuh for wa / wb).
 struct Cell2 {
   V2 U[5];
   V2 F[5];
-  V2 u;
-  V2 c;
+  V2 wa;
+  V2 wb;
 };
 
 __device__ __forceinline__ V2 v2(float x, float y) { return make_float2(x, y); }
@@ -84,19 +85,20 @@ struct FastPair {
     o.F[3] = mul(U[3], ud);
     o.F[4] = mul(add(U[4], p), ud);
     o.F[VEL] = fma(U[VEL], ud, p);
-    o.u = ud;
-    o.c = sqrt_(mul(mul(splat(k.g), p), ir));
+    const V2 c = sqrt_(mul(mul(splat(k.g), p), ir));
+    o.wa = add(ud, c);
+    o.wb = sub(c, ud);
   }
 
+  // FastPolicy::hll on both cells
   static __device__ __forceinline__ void hll(const Cell2& L, const Cell2& R, V2 F[5]) {
-    V2 sp = vmax(vmax(add(L.u, L.c), add(R.u, R.c)), splat(0.f));
-    V2 sm = vmin(vmin(sub(L.u, L.c), sub(R.u, R.c)), splat(0.f));
-    V2 inv = rcp(sub(sp, sm));
-    V2 a = mul(sp, inv), b = mul(sm, inv);
-    V2 s = mul(sm, a);
-    V2 nb = mul(b, splat(-1.f));
+    V2 sp = vmax(vmax(L.wa, R.wa), splat(0.f));
+    V2 ns = vmax(vmax(L.wb, R.wb), splat(0.f));
+    V2 inv = rcp(add(sp, ns));
+    V2 a = mul(sp, inv), b = mul(ns, inv);
+    V2 s = mul(ns, a);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) F[i] = fma(a, L.F[i], fma(nb, R.F[i], mul(s, sub(R.U[i], L.U[i]))));
+    for (int i = 0; i < 5; ++i) F[i] = fma(a, L.F[i], fma(b, R.F[i], mul(s, sub(L.U[i], R.U[i]))));
   }
 
   static __device__ __forceinline__ void update(const Cell2& C, const V2 flo[5], const V2 fhi[5],
@@ -134,23 +136,23 @@ struct ExactPair {
     Cell<float> r;
 #pragma unroll
     for (int i = 0; i < 5; ++i) { r.U[i] = c.U[i].x; r.F[i] = c.F[i].x; }
-    r.u = c.u.x;
-    r.c = c.c.x;
+    r.wa = c.wa.x;
+    r.wb = c.wb.x;
     return r;
   }
   static __device__ __forceinline__ Cell<float> hi(const Cell2& c) {
     Cell<float> r;
 #pragma unroll
     for (int i = 0; i < 5; ++i) { r.U[i] = c.U[i].y; r.F[i] = c.F[i].y; }
-    r.u = c.u.y;
-    r.c = c.c.y;
+    r.wa = c.wa.y;
+    r.wb = c.wb.y;
     return r;
   }
   static __device__ __forceinline__ void join(Cell2& o, const Cell<float>& a, const Cell<float>& b) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) { o.U[i] = v2(a.U[i], b.U[i]); o.F[i] = v2(a.F[i], b.F[i]); }
-    o.u = v2(a.u, b.u);
-    o.c = v2(a.c, b.c);
+    o.wa = v2(a.wa, b.wa);
+    o.wb = v2(a.wb, b.wb);
   }
   static __device__ __forceinline__ void split(const V2 s[5], float a[5], float b[5]) {
 #pragma unroll
