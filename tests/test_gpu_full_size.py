@@ -1,0 +1,68 @@
+"""The 512^3 benchmark workload (shear layer, the bench's default) at full size.
+
+Size-independent properties of the fused step on the full grid, and one exact
+step against the C oracle bit for bit (the oracle finishes a 512^3 step in a
+couple of seconds on the host cores).
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+GAMMA = 5.0 / 3.0
+N = 512
+
+
+@pytest.fixture(scope="module")
+def shear(tg):
+    W, dx = tg.shear_layer(N, seed=0)
+    dt = float(tg._cfl_time_step(W, dx, GAMMA))
+    return W, dx, dt
+
+
+def test_exact_step_bit_identical_to_oracle(tg, oracle_lib, shear):
+    W, dx, dt = shear
+    out = tg._evolve_state(W, dx, dt, GAMMA, exact=True)
+    ref = oracle_lib._evolve_state(W.cpu().numpy(), dx, np.float32(dt), GAMMA)
+    assert np.array_equal(out.cpu().numpy(), ref)
+
+
+def test_cfl_dt_matches_oracle(tg, oracle_lib, shear):
+    W, dx, dt = shear
+    assert np.float32(dt) == oracle_lib._cfl_time_step(W.cpu().numpy(), dx, GAMMA)
+
+
+def test_tile_shapes_agree(tg, shear):
+    W, dx, dt = shear
+    ref = tg._evolve_state(W, dx, dt, GAMMA)
+    for tile in ((8, 64), (32, 128), (16, 7)):
+        assert torch.equal(tg._evolve_state(W, dx, dt, GAMMA, tile=tile), ref), tile
+
+
+def test_fused_equals_three_sweeps(tg, shear):
+    W, dx, dt = shear
+    fused = tg._evolve_state(W, dx, dt, GAMMA)
+    a = tg._evolve_state_along_axis(W, dx, dt, GAMMA, 1, conserved_out=True)
+    b = tg._evolve_state_along_axis(a, dx, dt, GAMMA, 2, conserved_in=True, conserved_out=True)
+    del a
+    c = tg._evolve_state_along_axis(b, dx, dt, GAMMA, 3, conserved_in=True)
+    assert torch.equal(fused, c)
+
+
+def test_roll_equivariance(tg, shear):
+    W, dx, dt = shear
+    shifts, dims = (7, -13, 29), (1, 2, 3)
+    a = tg._evolve_state(torch.roll(W, shifts, dims), dx, dt, GAMMA)
+    b = torch.roll(tg._evolve_state(W, dx, dt, GAMMA), shifts, dims)
+    assert torch.equal(a, b)
+
+
+def test_run_conserves_totals(tg, shear):
+    W, dx, _ = shear
+    t0, _ = tg.diagnostics.diagnostics(W, GAMMA, slices=False)
+    out, t1, sl = tg.diagnostics.run_steps_with_diagnostics(W, dx, GAMMA, 10)
+    scale, _ = tg.diagnostics.diagnostics(out.abs(), GAMMA, slices=False)
+    drift = ((t1 - t0).abs() / scale).cpu().numpy()
+    assert drift.max() < 1e-6, drift
+    assert torch.equal(sl[0], out[0, :, :, N // 2])
