@@ -100,7 +100,10 @@ int tf_cfl_time_step(const float *W, int nx, int ny, int nz, float dx, float gam
 
 /* fluid.py:562-578 _evolve_state: one split step with a given dt.  dt is
  * read from dt_dev (device float) when non-NULL, else dt_host.  flags:
- * TF_FLAG_OPEN_BOUNDARIES, TF_FLAG_EXACT.  tile may be NULL. */
+ * TF_FLAG_OPEN_BOUNDARIES, TF_FLAG_EXACT; or TF_FLAG_IN_CONSERVED |
+ * TF_FLAG_OUT_CONSERVED together (fast arithmetic, 16-row tiles): a conserved
+ * state in and out, equal bit for bit to the three conserved fast sweeps.
+ * tile may be NULL. */
 int tf_evolve_state(const float *W_in, float *W_out, int nx, int ny, int nz, float dx,
                     float dt_host, const float *dt_dev, float gamma, unsigned flags,
                     const tf_tile_config *tile, void *stream);

@@ -175,6 +175,23 @@ def test_fast_fused_step_equals_fast_sweeps(tg, shape, hb):
     assert torch.equal(fused, c)
 
 
+@pytest.mark.parametrize("shape", [(5, 7, 33), (40, 31, 64), (1, 1, 1)])
+def test_fused_conserved_step_equals_conserved_sweeps(tg, shape):
+    """The conserved-in/out fused step (the adjoint's forward pass) equals the
+    three conserved fast sweeps bit for bit."""
+    U = tg.conserved_state_from_primitive(dev(random_state(shape, 41)), GAMMA)
+    dt = 2e-3
+    fused = tg._evolve_state(U, 0.05, dt, GAMMA, conserved=True)
+    a = tg._evolve_state_along_axis(U, 0.05, dt, GAMMA, 1, conserved_in=True, conserved_out=True)
+    b = tg._evolve_state_along_axis(a, 0.05, dt, GAMMA, 2, conserved_in=True, conserved_out=True)
+    c = tg._evolve_state_along_axis(b, 0.05, dt, GAMMA, 3, conserved_in=True, conserved_out=True)
+    assert torch.equal(fused, c)
+    with pytest.raises(tg.TinyfluidsError):
+        tg._evolve_state(U, 0.05, dt, GAMMA, conserved=True, exact=True)
+    with pytest.raises(tg.TinyfluidsError):
+        tg._evolve_state(U, 0.05, dt, GAMMA, conserved=True, tile=(8, 4))
+
+
 @pytest.mark.parametrize("axis,shift", [(1, 3), (2, -5), (3, 31)])
 def test_fast_step_roll_equivariant(tg, axis, shift):
     W = random_state((40, 36, 70), 12)

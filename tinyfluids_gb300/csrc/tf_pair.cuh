@@ -125,6 +125,22 @@ struct FastPair {
   }
 };
 
+// FastPair on conserved input and output: the fused step on states that are
+// already conserved (the adjoint's forward passes).  Same operations as
+// FastPair between the two conversions, so a step equals the three
+// conserved-in/out fast sweeps bit for bit.  The CFL speed is not formed.
+struct FastPairConserved : FastPair {
+  static __device__ __forceinline__ void to_state(const V2 w[5], V2 U[5], const StepConsts<float>&) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) U[i] = w[i];
+  }
+  static __device__ __forceinline__ V2 finish(const V2 U[5], V2 w[5], const StepConsts<float>&) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) w[i] = U[i];
+    return splat(0.f);
+  }
+};
+
 // ---------------------------------------------------------------------------
 // ExactPair: ExactPolicy<float> on each component.
 // ---------------------------------------------------------------------------

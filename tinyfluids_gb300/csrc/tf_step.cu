@@ -225,6 +225,7 @@ struct FusedArgs {
   int loop;        // 1: predicated loop step (parity buffers, dt from ctl)
   double* totals;  // diagnostics instantiation: conserved totals (zeroed before)
   DiagArgs diag;   // diagnostics instantiation: optional slice
+  int conserved_io;  // fast policy on conserved input and output (16-row tiles)
 };
 
 template <class P, int NWP, bool DIAG = false>
@@ -468,6 +469,13 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
       else fused_step_kernel<FastPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
     });
     return launch_check("fused_step_kernel (diagnostics)");
+  }
+  if (a.conserved_io) {
+    if (exact || rows != 16)
+      return set_error(TF_ERR_UNSUPPORTED,
+                       "conserved input/output: fast arithmetic and 16-row tiles only");
+    fused_step_kernel<FastPairConserved, 8><<<grid, 8 * 32, 0, s>>>(a);
+    return launch_check("fused_step_kernel (conserved)");
   }
   TF_DISPATCH_ROWS(rows, NWP, {
     if (exact) fused_step_kernel<ExactPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
@@ -737,6 +745,13 @@ int tf_evolve_state(const float* W_in, float* W_out, int nx, int ny, int nz, flo
   a.dt_dev = dt_dev;
   a.loop = 0;
   a.ctl = nullptr;
+  const unsigned cons = TF_FLAG_IN_CONSERVED | TF_FLAG_OUT_CONSERVED;
+  if (flags & cons) {
+    if ((flags & cons) != cons)
+      return set_error(TF_ERR_UNSUPPORTED, "the fused step takes conserved input and output together");
+    a.conserved_io = 1;
+    loader = 1;
+  }
   return launch_fused(a, rows, (flags & TF_FLAG_EXACT) != 0, (cudaStream_t)stream, loader);
 }
 

@@ -262,19 +262,25 @@ def _cfl_time_step(primitive_state, grid_spacing, gamma, C_CFL=0.4):
 # fluid.py:508-578
 # ---------------------------------------------------------------------------
 def _evolve_state(primitive_state, grid_spacing, dt, gamma, handle_boundaries=False, *,
-                  exact=None, tile=None):
+                  exact=None, tile=None, conserved=False):
     """fluid.py:562-578: optional open boundaries, then the x, y, z HLL sweeps,
     fused into one kernel pass.  ``dt`` is a float or a 0-d CUDA tensor (for
-    example the result of :func:`_cfl_time_step`)."""
+    example the result of :func:`_cfl_time_step`).  ``conserved=True`` (fast
+    arithmetic, default tile): the state in and out is conserved (rho, m, E),
+    equal bit for bit to three ``_evolve_state_along_axis`` sweeps with
+    conserved input and output."""
     W = check_state(primitive_state)
     _, nx, ny, nz = W.shape
+    flags = _flags(handle_boundaries, exact)
+    if conserved:
+        flags |= _lib.TF_FLAG_IN_CONSERVED | _lib.TF_FLAG_OUT_CONSERVED
     with torch.cuda.device(W.device):
         out = torch.empty_like(W)
         dt_host, dt_dev, keep = _dt_args(dt, W.device)
-        tc = _tile_arg(tile, W, exact)
+        tc = None if conserved and tile is None else _tile_arg(tile, W, exact)
         _lib.call("tf_evolve_state", W.data_ptr(), out.data_ptr(), nx, ny, nz,
                   float(grid_spacing), dt_host, dt_dev, _scalar(gamma, "gamma"),
-                  _flags(handle_boundaries, exact), tc, _stream(W))
+                  flags, tc, _stream(W))
         del keep
     return out
 
