@@ -129,6 +129,16 @@ int tf_evolve_state_diag(const float *W_in, float *W_out, int nx, int ny, int nz
 int tf_diagnostics(const float *W, int nx, int ny, int nz, float gamma, double *totals,
                    float *slice, int z_slice, void *stream);
 
+/* Verification hooks of the checked build (compiled with TF_CHECKED=1; the
+ * product build returns TF_ERR_UNSUPPORTED / -1).  In a checked build the
+ * fused step range-checks every global load and store (out-of-range accesses
+ * are counted and skipped) and adds 1 to write_counts[cell] (ncells int32 of
+ * device memory, cell = (x*ny + y)*nz + z) for every cell it stores.  No
+ * reference counterpart (the reference has no race or bounds checking). */
+int tf_debug_checked(void);
+int tf_debug_reset(int *write_counts, long long ncells);
+long long tf_debug_oob_count(void);
+
 /* time_integration.py:94-128 (plain branch): while t < t_final: dt = CFL dt;
  * W = step(W, dt); t += dt; iter += 1.  max_steps >= 0 also bounds the loop
  * (0 = t_final only is NOT implied: pass -1 for unbounded).  fixed_dt > 0

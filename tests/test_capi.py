@@ -84,6 +84,12 @@ def test_host_side_argument_checks(lib):
                   None, None, None)
 
 
+def test_product_library_is_not_the_checked_build(lib):
+    assert lib.tf_debug_checked() == 0
+    assert lib.tf_debug_oob_count() == -1
+    assert lib.tf_debug_reset(None, 0) == 5  # TF_ERR_UNSUPPORTED
+
+
 def test_python_api_validates_before_launch():
     import torch
     import tinyfluids_gb300 as tg

@@ -13,6 +13,7 @@ from . import build as _build
 
 _LOCK = threading.Lock()
 _LIB = None
+_LIB_CHECKED = None
 
 c_int = ctypes.c_int
 c_uint = ctypes.c_uint
@@ -58,6 +59,9 @@ SIGNATURES = {
     "tf_evolve_state_diag": (c_int, [vp, vp, c_int, c_int, c_int, c_float, c_float, vp,
                                      c_float, c_uint, vp, vp, vp, c_int, vp]),
     "tf_diagnostics": (c_int, [vp, c_int, c_int, c_int, c_float, vp, vp, c_int, vp]),
+    "tf_debug_checked": (c_int, []),
+    "tf_debug_reset": (c_int, [vp, c_ll]),
+    "tf_debug_oob_count": (c_ll, []),
     "tf_time_integration": (c_int, [vp, vp, vp, vp, c_int, c_int, c_int, c_float, c_float,
                                     c_float, c_float, c_int, c_float, c_uint, vp, vp, vp]),
     "tf_evolve_along_axis": (c_int, [vp, vp, c_int, c_int, c_int, c_float, c_float, vp,
@@ -129,6 +133,25 @@ def load():
             raise RuntimeError("tinyfluids_gb300 library ABI mismatch")
         _LIB = L
     return _LIB
+
+
+def load_checked():
+    """The checked build of the library (TF_CHECKED=1: range-checked accesses
+    and per-cell write counts), built on first use into its own file.  A
+    separate handle: the product library stays the one ``call`` uses."""
+    global _LIB_CHECKED
+    with _LOCK:
+        if _LIB_CHECKED is None:
+            path = _build.build(checked=True)
+            L = ctypes.CDLL(path)
+            for name, (res, args) in SIGNATURES.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            if L.tf_debug_checked() != 1:
+                raise RuntimeError("the checked library was not built with TF_CHECKED=1")
+            _LIB_CHECKED = L
+    return _LIB_CHECKED
 
 
 def call(name, *args):

@@ -20,6 +20,10 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB_NAME = "libtinyfluids_gb300.so"
 LIB = os.path.join(OUT_DIR, LIB_NAME)
+# the checked build (TF_CHECKED=1): range-checked accesses and per-cell write
+# counts for the tests; never loaded by the package itself
+LIB_CHECKED = os.path.join(OUT_DIR, "libtinyfluids_gb300_checked.so")
+OBJ_DIR_CHECKED = os.path.join(OUT_DIR, "obj_checked")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -42,23 +46,28 @@ def _deps():
             sorted(glob.glob(os.path.join(INCLUDE, "*.h"))) + [os.path.abspath(__file__)])
 
 
-def is_stale() -> bool:
-    if not os.path.exists(LIB):
+def is_stale(lib: str = LIB) -> bool:
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return any(os.path.getmtime(d) > t for d in _deps())
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
-    """Compile (if stale) and return the path of the shared library."""
-    if not force and not is_stale():
-        return LIB
+def build(force: bool = False, verbose: bool = False, extra_flags=None,
+          checked: bool = False) -> str:
+    """Compile (if stale) and return the path of the shared library
+    (``checked=True``: the TF_CHECKED=1 verification build)."""
+    lib = LIB_CHECKED if checked else LIB
+    obj_dir = OBJ_DIR_CHECKED if checked else OBJ_DIR
+    if not force and not is_stale(lib):
+        return lib
     nvcc = _nvcc()
-    os.makedirs(OBJ_DIR, exist_ok=True)
-    flags = ARCH + NVCC_FLAGS + ["-I", INCLUDE] + list(extra_flags or [])
+    os.makedirs(obj_dir, exist_ok=True)
+    flags = (ARCH + NVCC_FLAGS + ["-I", INCLUDE] + (["-DTF_CHECKED=1"] if checked else [])
+             + list(extra_flags or []))
 
     def compile_one(src):
-        obj = os.path.join(OBJ_DIR, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(obj_dir, os.path.basename(src)[:-3] + ".o")
         cmd = [nvcc, *flags, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -70,13 +79,13 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 1))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + f".tmp{os.getpid()}"
+    tmp = lib + f".tmp{os.getpid()}"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -109,9 +109,33 @@ __device__ __forceinline__ void diag_cell(TileOut& o, int x, int sy, const V2 wo
   }
 }
 
+// Checked build (TF_CHECKED=1, a separate library used by the tests): every
+// global load and store of the fused tile is range-checked -- an access
+// outside the state is counted and skipped, never performed -- and every
+// stored cell increments its entry of a caller-provided write-count array,
+// so a test sees that each cell of a step is written exactly once (no two
+// tiles store the same cell, none is missed).  The product build compiles
+// none of this.
+#ifndef TF_CHECKED
+#define TF_CHECKED 0
+#endif
+#if TF_CHECKED
+static __device__ unsigned long long g_chk_oob;
+static __device__ int* g_chk_writes;
+static __device__ long long g_chk_ncells;
+#endif
+
 __device__ __forceinline__ void store5(const TileOut& o, int x, size_t dcol, const V2 wo[5],
                                        bool hi) {
   float* q = o.dst + (size_t)x * o.plane + dcol;
+#if TF_CHECKED
+  const size_t cell = (size_t)x * o.plane + dcol;
+  if (cell >= o.vstride) {
+    atomicAdd(&g_chk_oob, 1ull);
+    return;
+  }
+  if (g_chk_writes && (long long)cell < g_chk_ncells) atomicAdd(g_chk_writes + cell, 1);
+#endif
 #pragma unroll
   for (int i = 0; i < 5; ++i) q[i * o.vstride] = hi ? wo[i].y : wo[i].x;
 }
@@ -284,7 +308,18 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
     o.sy_b = on && o.store_b ? t.yb : -1;
   }
   const bool open = G.open_bc != 0;
+#if TF_CHECKED
+  const size_t total = 5 * o.vstride;
+  auto ld = [&](const float* p) {
+    if ((size_t)(p - src) >= total) {
+      atomicAdd(&g_chk_oob, 1ull);
+      return 0.f;
+    }
+    return COHERENT ? __ldcg(p) : __ldg(p);
+  };
+#else
   auto ld = [&](const float* p) { return COHERENT ? __ldcg(p) : __ldg(p); };
+#endif
   auto load = [&](int x, V2 v[5]) {
     const float* p = src + (size_t)src_index(x, G.nx, open) * o.plane;
 #pragma unroll

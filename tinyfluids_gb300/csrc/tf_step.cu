@@ -782,6 +782,34 @@ int tf_evolve_state_diag(const float* W_in, float* W_out, int nx, int ny, int nz
   return launch_fused(a, rows, (flags & TF_FLAG_EXACT) != 0, s, 1);
 }
 
+int tf_debug_checked(void) { return TF_CHECKED; }
+
+int tf_debug_reset(int* write_counts, long long ncells) {
+#if TF_CHECKED
+  unsigned long long zero = 0;
+  TF_TRY(cuda_check(cudaMemcpyToSymbol(g_chk_oob, &zero, sizeof zero), "cudaMemcpyToSymbol"));
+  TF_TRY(cuda_check(cudaMemcpyToSymbol(g_chk_writes, &write_counts, sizeof write_counts),
+                    "cudaMemcpyToSymbol"));
+  TF_TRY(cuda_check(cudaMemcpyToSymbol(g_chk_ncells, &ncells, sizeof ncells),
+                    "cudaMemcpyToSymbol"));
+  return TF_OK;
+#else
+  (void)write_counts;
+  (void)ncells;
+  return set_error(TF_ERR_UNSUPPORTED, "not a checked build (TF_CHECKED=0)");
+#endif
+}
+
+long long tf_debug_oob_count(void) {
+#if TF_CHECKED
+  unsigned long long v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_chk_oob, sizeof v) != cudaSuccess) return -1;
+  return (long long)v;
+#else
+  return -1;
+#endif
+}
+
 int tf_diagnostics(const float* W, int nx, int ny, int nz, float gamma, double* totals,
                    float* slice, int z_slice, void* stream) {
   if (!W || !totals) return set_error(TF_ERR_ARG, "null pointer");
