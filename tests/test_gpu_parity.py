@@ -133,6 +133,18 @@ def test_graph_loop_matches_host_loop(tg, shape, t_final):
     assert int(ic) == int(ia) and torch.equal(c, a)
 
 
+@pytest.mark.parametrize("hb", [False, True])
+def test_step_is_one_loop_iteration(tg, oracle_lib, hb):
+    W = dev(random_state((20, 24, 28), 13))
+    out, dt = tg.step(W, 0.05, GAMMA, 0.4, hb, return_dt=True)
+    assert torch.equal(out, tg.run_steps(W, 0.05, GAMMA, 1, hb))
+    assert torch.equal(out, tg._evolve_state(W, 0.05, dt, GAMMA, hb))
+    ex, dte = tg.step(W, 0.05, GAMMA, 0.4, hb, exact=True, return_dt=True)
+    ref, rit = oracle_lib.time_integration(host(W), 0.05, float("inf"), GAMMA, hb, max_steps=1)
+    assert rit == 1 and np.array_equal(host(ex), ref)
+    assert float(dte) == float(oracle_lib._cfl_time_step(host(W), 0.05, GAMMA))
+
+
 def test_setup_ics_matches_reference_builder(tg):
     W, dx = tg.setup_ics(40, 40 // 16)
     Wn, dxn = I.setup_ics(40, 40 // 16)

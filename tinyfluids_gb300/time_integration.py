@@ -52,6 +52,19 @@ def run_steps(primitive_state, grid_spacing, gamma, num_steps, handle_boundaries
     return (W, ctl) if return_ctl else W
 
 
+def step(primitive_state, grid_spacing, gamma, C_CFL=0.4, handle_boundaries=False, *,
+         exact=None, tile=None, return_dt=False):
+    """One loop iteration: dt = CFL dt of the state (fluid.py:427-504), then
+    the split step (fluid.py:562-578); the same bits as ``run_steps(..., 1)``.
+    With ``return_dt`` also returns the dt used (0-d float32 CUDA tensor)."""
+    W, ctl = run_steps(primitive_state, grid_spacing, gamma, 1, handle_boundaries, C_CFL=C_CFL,
+                       exact=exact, tile=tile, return_ctl=True)
+    if not return_dt:
+        return W
+    # the loop's t after one step is the dt it took
+    return W, ctl.view(torch.float32)[CTL_T].clone()
+
+
 def _run(primitive_state, grid_spacing, gamma, t_final, max_steps, fixed_dt,
          handle_boundaries, C_CFL, exact, tile, wait, host_loop=False):
     W = check_state(primitive_state)
