@@ -113,7 +113,7 @@ def test_exact_time_integration_reproduces_reference_counts(tg, oracle_lib, n, h
         assert np.array_equal(host(Wf), ref)
 
 
-@pytest.mark.parametrize("n", [32, 64, 96, 128])
+@pytest.mark.parametrize("n", [32, 64, 96, 128, 196, 256])
 def test_fast_time_integration_reproduces_reference_counts(tg, n):
     W, dx = tg.setup_ics(n, n // 16)
     _, it = tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False)
