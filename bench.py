@@ -178,7 +178,7 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "ms_per_step": 1e3 * args.n ** 3 / (cb["value"] * 1e9),
             "config": {"workload": f"shear layer {args.n}^3, gamma=5/3, CFL 0.4, periodic",
-                       "global_batch": 1, "seq_len": None, "parallelism": "cpu"},
+                       "instances": 1, "parallelism": "cpu"},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
@@ -294,10 +294,12 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"shear layer {n}^3, gamma=5/3, CFL 0.4, periodic, "
                                f"{K} steps per run",
-                   "global_batch": world, "seq_len": None,
+                   "instances": world,
                    "parallelism": "replicas" if world > 1 else "single",
                    "arithmetic": "exact" if args.exact else "fast",
-                   "l2": "state 2.7 GB >> 129 MB L2 (no flush needed)",
+                   "l2": f"state {20 * n ** 3 / 1e9:.2f} GB vs 129 MB L2"
+                         + (" (no flush needed)" if 2 * 20 * n ** 3 > 129e6 else
+                            " (state fits in L2: not a DRAM measurement)"),
                    "tile": list(tile) if tile else "heuristic"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
