@@ -64,6 +64,13 @@ def test_host_side_argument_checks(lib):
     other = ctypes.c_void_p(0x2000)
     with pytest.raises(_lib.TinyfluidsError):  # zero-size axis
         _lib.call("tf_evolve_state", fake, other, 0, 4, 4, 0.1, 0.01, None, 5 / 3, 0, None, None)
+    with pytest.raises(_lib.TinyfluidsError):  # above the 2^40-cell limit
+        _lib.call("tf_evolve_state", fake, other, 1 << 14, 1 << 14, 1 << 14, 0.1, 0.01, None,
+                  5 / 3, 0, None, None)
+    with pytest.raises(_lib.TinyfluidsError):  # tile grid beyond the launch limits
+        tc2 = _lib.TileConfig(8, 1, 0)
+        _lib.call("tf_evolve_state", fake, other, 1 << 17, 8, 8, 0.1, 0.01, None, 5 / 3, 0,
+                  ctypes.byref(tc2), None)
     with pytest.raises(_lib.TinyfluidsError):  # open boundaries need 2 cells
         _lib.call("tf_evolve_state", fake, other, 1, 4, 4, 0.1, 0.01, None, 5 / 3, 1, None, None)
     with pytest.raises(_lib.TinyfluidsError):  # gamma == 1

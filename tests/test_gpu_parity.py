@@ -248,6 +248,14 @@ def test_nonfinite_state_is_reported(tg, host_loop):
     assert e.value.status == 3
 
 
+def test_empty_axis_rejected(tg):
+    with pytest.raises(ValueError):
+        tg._evolve_state(torch.zeros(5, 0, 4, 4, device="cuda"), 0.1, 1e-3, GAMMA)
+    with pytest.raises(ValueError):
+        tg.time_integration_fn(torch.zeros(5, 4, 4, 0, device="cuda"), 0.1, 0.1, GAMMA, False,
+                               False)
+
+
 def test_time_integration_zero_and_negative_t_final(tg):
     W = dev(random_state((6, 6, 6), 3))
     Wf, it = tg.time_integration_fn(W, 0.1, 0.0, GAMMA, False, False)
