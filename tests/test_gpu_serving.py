@@ -74,6 +74,14 @@ def test_srpt_finishes_least_remaining_work_first(tg):
         Server(policy="lifo")
 
 
+def test_budget_from_free_hbm(tg):
+    free, _ = torch.cuda.mem_get_info()
+    srv = Server(hbm_budget=None)
+    assert 0 < srv.budget <= free
+    done = srv.serve([Request(0, 24, 5, "overpressure", 1, 0.0)])
+    assert len(done) == 1 and srv.used == 0
+
+
 def test_oversized_request_rejected(tg):
     srv = Server(hbm_budget=1e6)
     with pytest.raises(ValueError):

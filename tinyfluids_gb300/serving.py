@@ -78,6 +78,9 @@ class _Active:
 class Server:
     """Admits requests by free HBM budget and advances admitted ones together.
 
+    hbm_budget: bytes of request state the server may hold (two state buffers
+    per request); None takes 90% of the HBM free when the server is created.
+
     A tick advances a set of active requests by min(tick_steps, remaining)
     steps each, in one persistent batch launch.  policy "all" puts every
     active request in every tick (processor sharing).  policy "srpt" (the
@@ -104,6 +107,11 @@ class Server:
         self.policy = policy
         self.tick_budget = int(tick_budget)
         self.device = torch.device(device if device is not None else "cuda")
+        if hbm_budget is None:
+            # admit by the HBM actually free now, keeping 10% for the batch
+            # plans' workspaces and the allocator's slack
+            free, _ = torch.cuda.mem_get_info(self.device)
+            hbm_budget = 0.9 * free
         self.budget = int(hbm_budget)
         self.tick_steps = int(tick_steps) | 1
         self.rows = rows
