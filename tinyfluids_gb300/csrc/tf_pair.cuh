@@ -34,26 +34,11 @@ __device__ __forceinline__ V2 splat(float x) { return make_float2(x, x); }
 // ---------------------------------------------------------------------------
 struct FastPair {
   static constexpr bool kExact = false;
-#ifndef TF_SCALAR_PAIRS
   static __device__ __forceinline__ V2 add(V2 a, V2 b) { return __fadd2_rn(a, b); }
   static __device__ __forceinline__ V2 mul(V2 a, V2 b) { return __fmul2_rn(a, b); }
   static __device__ __forceinline__ V2 fma(V2 a, V2 b, V2 c) { return __ffma2_rn(a, b, c); }
   // a - b rounded once: b * (-1) is exact
   static __device__ __forceinline__ V2 sub(V2 a, V2 b) { return __ffma2_rn(b, splat(-1.f), a); }
-#else  // the same ops on each component (same results, scalar instructions)
-  static __device__ __forceinline__ V2 add(V2 a, V2 b) {
-    return v2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
-  }
-  static __device__ __forceinline__ V2 mul(V2 a, V2 b) {
-    return v2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
-  }
-  static __device__ __forceinline__ V2 fma(V2 a, V2 b, V2 c) {
-    return v2(__fmaf_rn(a.x, b.x, c.x), __fmaf_rn(a.y, b.y, c.y));
-  }
-  static __device__ __forceinline__ V2 sub(V2 a, V2 b) {
-    return v2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y));
-  }
-#endif
   static __device__ __forceinline__ V2 vmax(V2 a, V2 b) { return v2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
   static __device__ __forceinline__ V2 vmin(V2 a, V2 b) { return v2(fminf(a.x, b.x), fminf(a.y, b.y)); }
   static __device__ __forceinline__ V2 rcp(V2 a) { return v2(FastPolicy::rcp(a.x), FastPolicy::rcp(a.y)); }
