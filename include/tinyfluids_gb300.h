@@ -136,6 +136,10 @@ int tf_diagnostics(const float *W, int nx, int ny, int nz, float gamma, double *
  * device memory, cell = (x*ny + y)*nz + z) for every cell it stores.  No
  * reference counterpart (the reference has no race or bounds checking). */
 int tf_debug_checked(void);
+/* Evaluation cap of the device-side t_final loop for graphs built from now
+ * on (cap <= 0 or above the default restores the default 2^24): lets a test
+ * run a loop into its bound. */
+int tf_debug_set_graph_loop_cap(int cap);
 int tf_debug_reset(int *write_counts, long long ncells);
 long long tf_debug_oob_count(void);
 

@@ -248,6 +248,22 @@ def test_nonfinite_state_is_reported(tg, host_loop):
     assert e.value.status == 3
 
 
+def test_graph_loop_stops_at_its_evaluation_cap(tg):
+    """The device-side while loop ends after `cap` condition evaluations even
+    though t_final is not reached: TF_ERR_TIMEOUT, exactly cap steps."""
+    W, dx = tg.setup_ics(32, 2)
+    lib = tg._lib.load()
+    lib.tf_debug_set_graph_loop_cap(5)
+    try:
+        with pytest.raises(tg.TinyfluidsError) as e:
+            tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False)
+        assert e.value.status == 4 and "after 5 steps" in str(e.value)
+    finally:
+        lib.tf_debug_set_graph_loop_cap(0)
+    _, it = tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False)
+    assert int(it) == GOLDEN["counts"]["32"]
+
+
 def test_empty_axis_rejected(tg):
     with pytest.raises(ValueError):
         tg._evolve_state(torch.zeros(5, 0, 4, 4, device="cuda"), 0.1, 1e-3, GAMMA)

@@ -60,6 +60,7 @@ SIGNATURES = {
                                      c_float, c_uint, vp, vp, vp, c_int, vp]),
     "tf_diagnostics": (c_int, [vp, c_int, c_int, c_int, c_float, vp, vp, c_int, vp]),
     "tf_debug_checked": (c_int, []),
+    "tf_debug_set_graph_loop_cap": (c_int, [c_int]),
     "tf_debug_reset": (c_int, [vp, c_ll]),
     "tf_debug_oob_count": (c_ll, []),
     "tf_time_integration": (c_int, [vp, vp, vp, vp, c_int, c_int, c_int, c_float, c_float,

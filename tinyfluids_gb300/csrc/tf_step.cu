@@ -4,6 +4,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -116,6 +117,9 @@ __global__ void ctl_init_kernel(tf_ctl* ctl, float t_final, float cfl_dx, int ma
 // whatever the step kernel does.  ctl->reserved[0] counts evaluations,
 // reserved[1] holds the bits of t at the previous one.
 constexpr int kGraphLoopCap = 1 << 24;
+// the cap new loop graphs get (tf_debug_set_graph_loop_cap lowers it so a
+// test can run into it)
+static std::atomic<int> g_graph_loop_cap{kGraphLoopCap};
 
 __global__ void loop_cond_kernel(tf_ctl* ctl, cudaGraphConditionalHandle h, int cap) {
   const int evals = ctl->reserved[0] + 1;
@@ -491,7 +495,7 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
 // on the same buffers launches the cached graph.  An evicted graph is
 // destroyed at once; CUDA frees it after any in-flight launch completes.
 struct GraphKey {
-  int device, rows, exact;
+  int device, rows, exact, cap;
   FusedArgs a;  // zero-initialised, so padding compares equal
 };
 struct GraphEntry {
@@ -502,7 +506,7 @@ static std::mutex g_graph_mu;
 static std::vector<GraphEntry> g_graphs;  // most recently used last
 constexpr size_t kGraphCacheSize = 8;
 
-static int build_graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl,
+static int build_graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, int cap,
                             cudaGraphExec_t* out);
 
 static int graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, cudaStream_t s) {
@@ -511,6 +515,7 @@ static int graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, cud
   TF_TRY(cuda_check(cudaGetDevice(&k.device), "cudaGetDevice"));
   k.rows = rows;
   k.exact = exact ? 1 : 0;
+  k.cap = g_graph_loop_cap.load();
   k.a = a;
   std::lock_guard<std::mutex> lk(g_graph_mu);
   for (size_t i = 0; i < g_graphs.size(); ++i) {
@@ -522,7 +527,7 @@ static int graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, cud
     }
   }
   cudaGraphExec_t exec = nullptr;
-  TF_TRY(build_graph_loop(a, rows, exact, ctl, &exec));
+  TF_TRY(build_graph_loop(a, rows, exact, ctl, k.cap, &exec));
   int st = cuda_check(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
   if (st != TF_OK) {
     cudaGraphExecDestroy(exec);
@@ -536,7 +541,7 @@ static int graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, cud
   return TF_OK;
 }
 
-static int build_graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl,
+static int build_graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, int cap,
                             cudaGraphExec_t* out) {
   cudaGraph_t g = nullptr, body = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -555,7 +560,6 @@ static int build_graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ct
     cudaGraphNode_t entry;
     cudaKernelNodeParams kp;
     memset(&kp, 0, sizeof kp);
-    int cap = kGraphLoopCap;
     void* cargs[3] = {(void*)&ctl, (void*)&h, (void*)&cap};
     kp.func = (void*)loop_cond_kernel;
     kp.gridDim = dim3(1);
@@ -579,7 +583,7 @@ static int build_graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ct
       break;
     int lst = launch_fused(a, rows, exact, cs, 1);
     if (lst == TF_OK) {
-      loop_cond_kernel<<<1, 1, 0, cs>>>(ctl, h, kGraphLoopCap);
+      loop_cond_kernel<<<1, 1, 0, cs>>>(ctl, h, cap);
       lst = launch_check("loop_cond_kernel");
     }
     cudaGraph_t captured = nullptr;
@@ -783,6 +787,11 @@ int tf_evolve_state_diag(const float* W_in, float* W_out, int nx, int ny, int nz
 }
 
 int tf_debug_checked(void) { return TF_CHECKED; }
+
+int tf_debug_set_graph_loop_cap(int cap) {
+  g_graph_loop_cap.store(cap > 0 && cap < kGraphLoopCap ? cap : kGraphLoopCap);
+  return TF_OK;
+}
 
 int tf_debug_reset(int* write_counts, long long ncells) {
 #if TF_CHECKED
