@@ -168,7 +168,10 @@ class Server:
             specs = [InstanceSpec(a.cur, a.dx, a.req.gamma,
                                   num_steps=min(self.tick_steps, a.remaining), C_CFL=self.cfl,
                                   out=a.other, consume_input=True) for a in group]
-            b = Batch(specs, rows=self.rows)
+            # a tick of one request runs as one launch per step (measured a
+            # few ms lower latency for lone requests); several share one
+            # persistent launch
+            b = Batch(specs, rows=self.rows, persistent=len(group) > 1)
             while len(self._plans) >= self._plan_cache:
                 old = self._plans.pop(next(iter(self._plans)))
                 old.close()
