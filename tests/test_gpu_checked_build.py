@@ -19,7 +19,9 @@ GAMMA = 5.0 / 3.0
 
 SHAPES = [(1, 1, 1), (2, 3, 5), (5, 7, 33), (33, 17, 61), (40, 31, 64), (3, 64, 29),
           (64, 15, 2), (31, 30, 32)]
-TILES = [None, (8, 3, 1), (16, 1, 1), (16, 5, 1), (32, 2, 1), (32, 7, 1)]
+# (rows, lx, loader): loader 1 = per-thread loads, 2 = TMA-staged planes
+# (falls back to loads when nz % 4 != 0); the TMA path's stores are counted
+TILES = [None, (8, 3, 1), (16, 1, 1), (16, 5, 1), (32, 2, 1), (32, 7, 1), (16, 5, 2), (32, 3, 2)]
 
 
 @pytest.fixture(scope="module")
