@@ -11,7 +11,9 @@
  *    rho, vx, vy, vz, p (fluid.py:10-22).  Conserved states use
  *    rho, mx, my, mz, E.
  *  - The caller owns all device memory; no entry point allocates device
- *    memory.  Inputs are never modified; outputs must not alias inputs.
+ *    memory for states or buffers (a t_final loop instantiates and caches a
+ *    CUDA graph, whose resources the CUDA driver holds).  Inputs are never
+ *    modified; outputs must not alias inputs.
  *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Work is
  *    enqueued asynchronously unless stated otherwise.
  *  - Every function returns a tf_status; tf_last_error() describes the last
