@@ -148,12 +148,33 @@ __global__ void __launch_bounds__(256) maxspeed_kernel(const float* __restrict__
                                                        float g, tf_ctl* ctl, int fast) {
   __shared__ float red[8];
   float m = 0.f;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    float w[5];
+  auto speed = [&](const float w[5]) {
+    return fast ? FastPolicy::cell_speed(w, g) : exact_cell_speed(w, g);
+  };
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  if ((n & 3) == 0 && (reinterpret_cast<uintptr_t>(W) & 15) == 0) {
+    // four cells per thread and variable with 16-byte loads: more bytes in
+    // flight per thread (the maximum does not depend on the visiting order)
+    const float4* W4 = reinterpret_cast<const float4*>(W);
+    const long long n4 = n >> 2;
+    for (long long i = t0; i < n4; i += stride) {
+      float4 v[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) w[v] = __ldg(W + v * n + i);
-    m = speed_max(m, fast ? FastPolicy::cell_speed(w, g) : exact_cell_speed(w, g));
+      for (int k = 0; k < 5; ++k) v[k] = __ldg(W4 + k * n4 + i);
+      const float a[5] = {v[0].x, v[1].x, v[2].x, v[3].x, v[4].x};
+      const float b[5] = {v[0].y, v[1].y, v[2].y, v[3].y, v[4].y};
+      const float c[5] = {v[0].z, v[1].z, v[2].z, v[3].z, v[4].z};
+      const float d[5] = {v[0].w, v[1].w, v[2].w, v[3].w, v[4].w};
+      m = speed_max(m, speed_max(speed_max(speed(a), speed(b)), speed_max(speed(c), speed(d))));
+    }
+  } else {
+    for (long long i = t0; i < n; i += stride) {
+      float w[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) w[v] = __ldg(W + v * n + i);
+      m = speed_max(m, speed(w));
+    }
   }
   float bm = block_max(m, red);
   if (threadIdx.x == 0) ctl_finish_cta(ctl, bm, gridDim.x, 0.f, false);
