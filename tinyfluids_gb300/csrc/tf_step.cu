@@ -59,30 +59,62 @@ static StepConsts<T> make_consts(T gamma, T dx, T dt) {
 // ---------------------------------------------------------------------------
 // conversions (fluid.py:30-103), exact arithmetic
 // ---------------------------------------------------------------------------
+// Cell-wise map of a [5][n] state: 16-byte loads and stores of four cells per
+// variable when n % 4 == 0 and both arrays are 16-byte aligned, else one
+// cell per thread.  `f(in[5], out[5])` maps one cell.
+template <class F>
+__device__ __forceinline__ void map_cells(const float* __restrict__ in, float* __restrict__ out,
+                                          long long n, F f) {
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  if ((n & 3) == 0 &&
+      ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0) {
+    const float4* in4 = reinterpret_cast<const float4*>(in);
+    float4* out4 = reinterpret_cast<float4*>(out);
+    const long long n4 = n >> 2;
+    for (long long i = t0; i < n4; i += stride) {
+      float4 v[5], r[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) v[k] = __ldg(in4 + k * n4 + i);
+      float a[5], b[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) a[k] = v[k].x;
+      f(a, b);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) r[k].x = b[k], a[k] = v[k].y;
+      f(a, b);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) r[k].y = b[k], a[k] = v[k].z;
+      f(a, b);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) r[k].z = b[k], a[k] = v[k].w;
+      f(a, b);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        r[k].w = b[k];
+        out4[k * n4 + i] = r[k];
+      }
+    }
+  } else {
+    for (long long i = t0; i < n; i += stride) {
+      float a[5], b[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) a[k] = in[k * n + i];
+      f(a, b);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) out[k * n + i] = b[k];
+    }
+  }
+}
+
 __global__ void cons_from_prim_kernel(const float* __restrict__ W, float* __restrict__ U,
                                       long long n, StepConsts<float> k) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    float w[5], u[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) w[v] = W[v * n + i];
-    exact_cons_from_prim(w, u, k);
-#pragma unroll
-    for (int v = 0; v < 5; ++v) U[v * n + i] = u[v];
-  }
+  map_cells(W, U, n, [&](const float w[5], float u[5]) { exact_cons_from_prim(w, u, k); });
 }
 
 __global__ void prim_from_cons_kernel(const float* __restrict__ U, float* __restrict__ W,
                                       long long n, StepConsts<float> k) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    float u[5], w[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) u[v] = U[v * n + i];
-    exact_prim_from_cons(u, w, k);
-#pragma unroll
-    for (int v = 0; v < 5; ++v) W[v * n + i] = w[v];
-  }
+  map_cells(U, W, n, [&](const float u[5], float w[5]) { exact_prim_from_cons(u, w, k); });
 }
 
 static int elementwise_grid(long long n) {
@@ -217,18 +249,44 @@ __global__ void __launch_bounds__(256) diagnostics_kernel(const float* __restric
   CSum acc[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) acc[v] = CSum{0.f, 0.f};
-  for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
-    const float* row = W + r * nz;
-    for (int z = threadIdx.x; z < nz; z += blockDim.x) {
-      float w[5], u[5];
+  auto cell = [&](const float w[5], long long r, int z) {
+    float u[5];
+    exact_cons_from_prim(w, u, k);
 #pragma unroll
-      for (int v = 0; v < 5; ++v) w[v] = __ldg(row + v * n + z);
-      exact_cons_from_prim(w, u, k);
+    for (int v = 0; v < 5; ++v) csum_add(acc[v], u[v]);
+    if (slice && z == z_slice) {
+      slice[r] = w[0];
+      slice[rows + r] = w[4];
+    }
+  };
+  if ((nz & 3) == 0 && (reinterpret_cast<uintptr_t>(W) & 15) == 0) {
+    // four cells of a row per thread with 16-byte loads
+    const int nz4 = nz >> 2;
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+      const float4* row = reinterpret_cast<const float4*>(W + r * nz);
+      const long long n4 = n >> 2;
+      for (int z4 = threadIdx.x; z4 < nz4; z4 += blockDim.x) {
+        float4 q[5];
 #pragma unroll
-      for (int v = 0; v < 5; ++v) csum_add(acc[v], u[v]);
-      if (slice && z == z_slice) {
-        slice[r] = w[0];
-        slice[rows + r] = w[4];
+        for (int v = 0; v < 5; ++v) q[v] = __ldg(row + v * n4 + z4);
+        const float a[5] = {q[0].x, q[1].x, q[2].x, q[3].x, q[4].x};
+        const float b[5] = {q[0].y, q[1].y, q[2].y, q[3].y, q[4].y};
+        const float c[5] = {q[0].z, q[1].z, q[2].z, q[3].z, q[4].z};
+        const float d[5] = {q[0].w, q[1].w, q[2].w, q[3].w, q[4].w};
+        cell(a, r, 4 * z4);
+        cell(b, r, 4 * z4 + 1);
+        cell(c, r, 4 * z4 + 2);
+        cell(d, r, 4 * z4 + 3);
+      }
+    }
+  } else {
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+      const float* row = W + r * nz;
+      for (int z = threadIdx.x; z < nz; z += blockDim.x) {
+        float w[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) w[v] = __ldg(row + v * n + z);
+        cell(w, r, z);
       }
     }
   }
@@ -850,8 +908,9 @@ int tf_diagnostics(const float* W, int nx, int ny, int nz, float gamma, double* 
   cudaStream_t s = (cudaStream_t)stream;
   TF_TRY(cuda_check(cudaMemsetAsync(totals, 0, 5 * sizeof(double), s), "cudaMemsetAsync"));
   const long long rows = (long long)nx * ny;
-  const long long cap = (long long)sm_count() * 8;
-  const int threads = nz >= 256 ? 256 : ((nz + 31) / 32) * 32;
+  const long long cap = (long long)sm_count() * 16;
+  const int per_row = (nz & 3) == 0 ? nz / 4 : nz;  // threads' work items per row
+  const int threads = per_row >= 256 ? 256 : ((per_row + 31) / 32) * 32;
   diagnostics_kernel<<<(int)(rows < cap ? rows : cap), threads, 0, s>>>(W, nx, ny, nz,
                                                          make_consts<float>(gamma, 1.f, 0.f),
                                                          totals, slice, z_slice);
