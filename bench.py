@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=512, help="grid size per axis")
     p.add_argument("--exact", action="store_true", help="reference op order (slower)")
-    p.add_argument("--e2e-repeats", type=int, default=2)
+    p.add_argument("--e2e-repeats", type=int, default=4)
     p.add_argument("--cpu-sample-seconds", type=float, default=20.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--tile", default=None, help="rows,lx of the fused kernel")
