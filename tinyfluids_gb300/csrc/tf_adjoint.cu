@@ -155,10 +155,9 @@ struct AdjGeom {
   int nx, ny, nz;
 };
 
-__device__ __forceinline__ long long nb_index(long long i, const AdjGeom& G, int vel, int d) {
-  int z = (int)(i % G.nz);
-  long long r = i / G.nz;
-  int y = (int)(r % G.ny), x = (int)(r / G.ny);
+// Linear index of the periodic neighbour at offset d along velocity index vel.
+__device__ __forceinline__ long long nb_index(int x, int y, int z, const AdjGeom& G, int vel,
+                                              int d) {
   if (vel == 1) x = wrap_index(x + d, G.nx);
   if (vel == 2) y = wrap_index(y + d, G.ny);
   if (vel == 3) z = wrap_index(z + d, G.nz);
@@ -173,9 +172,8 @@ __global__ void __launch_bounds__(256) adjoint_sweep_kernel(const T* __restrict_
                                                             T g) {
   const long long n = (long long)G.nx * G.ny * G.nz;
   const T gm1 = g - T(1);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long im = nb_index(i, G, VEL, -1), ip = nb_index(i, G, VEL, +1);
+  for_each_cell(G.nx, G.ny, G.nz, [&](long long i, int x, int y, int z) {
+    const long long im = nb_index(x, y, z, G, VEL, -1), ip = nb_index(x, y, z, G, VEL, +1);
     T u0[5], u1[5], u2[5], l0[5], l1[5], l2[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
@@ -204,7 +202,7 @@ __global__ void __launch_bounds__(256) adjoint_sweep_kernel(const T* __restrict_
     hll_vjp<T, VEL>(s1, s2, ghi, g, gm1, acc, dummy);  // cell i is the left state
 #pragma unroll
     for (int v = 0; v < 5; ++v) lam_in[v * n + i] = acc[v];
-  }
+  });
 }
 
 // Forward sweep in conserved variables, for the FP64 finite-difference check
@@ -215,9 +213,8 @@ __global__ void __launch_bounds__(256) cons_sweep_kernel(const T* __restrict__ U
                                                          T g) {
   const long long n = (long long)G.nx * G.ny * G.nz;
   const T gm1 = g - T(1);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long idx[3] = {nb_index(i, G, VEL, -1), i, nb_index(i, G, VEL, +1)};
+  for_each_cell(G.nx, G.ny, G.nz, [&](long long i, int x, int y, int z) {
+    const long long idx[3] = {nb_index(x, y, z, G, VEL, -1), i, nb_index(x, y, z, G, VEL, +1)};
     Side<T> s[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
@@ -231,7 +228,7 @@ __global__ void __launch_bounds__(256) cons_sweep_kernel(const T* __restrict__ U
     hll_forward(s[1], s[2], fhi);
 #pragma unroll
     for (int v = 0; v < 5; ++v) out[v * n + i] = fma(k, flo[v] - fhi[v], s[1].U[v]);
-  }
+  });
 }
 
 template <typename T>
@@ -244,20 +241,18 @@ static int launch_adj(bool adjoint, const T* U, const T* lam_out, T* out, int nx
   if (!(dx > 0) || !isfinite(dt) || !isfinite(gamma) || gamma == 1.0)
     return set_error(TF_ERR_ARG, "bad scalar parameter");
   AdjGeom G{nx, ny, nz};
-  long long n = (long long)nx * ny * nz;
-  long long b = (n + 255) / 256, cap = (long long)sm_count() * 8;
-  int grid = (int)(b < cap ? b : cap);
+  const RowLaunch rl = row_launch(nx, ny, nz);
   T k = (T)(dt / dx), g = (T)gamma;
   if (sizeof(T) == 4) k = (T)((float)dt * (1.f / (float)dx));  // as the fast sweep: dt * (1/dx)
   if (adjoint) {
-    if (axis == 0) adjoint_sweep_kernel<T, 1><<<grid, 256, 0, s>>>(U, lam_out, out, G, k, g);
-    if (axis == 1) adjoint_sweep_kernel<T, 2><<<grid, 256, 0, s>>>(U, lam_out, out, G, k, g);
-    if (axis == 2) adjoint_sweep_kernel<T, 3><<<grid, 256, 0, s>>>(U, lam_out, out, G, k, g);
+    if (axis == 0) adjoint_sweep_kernel<T, 1><<<rl.blocks, rl.threads, 0, s>>>(U, lam_out, out, G, k, g);
+    if (axis == 1) adjoint_sweep_kernel<T, 2><<<rl.blocks, rl.threads, 0, s>>>(U, lam_out, out, G, k, g);
+    if (axis == 2) adjoint_sweep_kernel<T, 3><<<rl.blocks, rl.threads, 0, s>>>(U, lam_out, out, G, k, g);
     return launch_check("adjoint_sweep_kernel");
   }
-  if (axis == 0) cons_sweep_kernel<T, 1><<<grid, 256, 0, s>>>(U, out, G, k, g);
-  if (axis == 1) cons_sweep_kernel<T, 2><<<grid, 256, 0, s>>>(U, out, G, k, g);
-  if (axis == 2) cons_sweep_kernel<T, 3><<<grid, 256, 0, s>>>(U, out, G, k, g);
+  if (axis == 0) cons_sweep_kernel<T, 1><<<rl.blocks, rl.threads, 0, s>>>(U, out, G, k, g);
+  if (axis == 1) cons_sweep_kernel<T, 2><<<rl.blocks, rl.threads, 0, s>>>(U, out, G, k, g);
+  if (axis == 2) cons_sweep_kernel<T, 3><<<rl.blocks, rl.threads, 0, s>>>(U, out, G, k, g);
   return launch_check("cons_sweep_kernel");
 }
 

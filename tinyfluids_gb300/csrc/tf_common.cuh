@@ -95,6 +95,18 @@ __device__ __forceinline__ void block_add_totals(const CSum acc[5], double* red,
   }
 }
 
+// Visits every cell (x, y, z) of an nx*ny*nz grid once: blocks stride over
+// the (x, y) rows, threads over z, so a cell's coordinates need no division
+// (one per row).  f(i, x, y, z) with i the linear index (x*ny + y)*nz + z.
+template <class F>
+__device__ __forceinline__ void for_each_cell(int nx, int ny, int nz, F f) {
+  const long long rows = (long long)nx * ny;
+  for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int y = (int)(r % ny), x = (int)(r / ny);
+    for (int z = threadIdx.x; z < nz; z += blockDim.x) f(r * nz + z, x, y, z);
+  }
+}
+
 // Volatile reads of control fields written by other kernels/CTAs.
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
 __device__ __forceinline__ float ld_volatile(const float* p) { return *(const volatile float*)p; }

@@ -21,6 +21,19 @@ inline int launch_check(const char* what) { return cuda_check(cudaGetLastError()
 
 int sm_count();  // multiprocessors of the current device (cached per device)
 
+// Launch shape of a for_each_cell kernel: threads along z (a multiple of 32,
+// at most 256), blocks over the (x, y) rows, at most 16 per SM.
+struct RowLaunch {
+  int blocks, threads;
+};
+inline RowLaunch row_launch(int nx, int ny, int nz) {
+  RowLaunch l;
+  l.threads = nz >= 256 ? 256 : ((nz + 31) / 32) * 32;
+  const long long rows = (long long)nx * ny, cap = (long long)sm_count() * 16;
+  l.blocks = (int)(rows < cap ? rows : cap);
+  return l;
+}
+
 }  // namespace tf
 
 // Tile heights (grid rows incl. the one-cell ring) the fused kernel is

@@ -712,12 +712,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(const float* __restrict__ sr
                                                     int out_prim, StepConsts<float> K) {
   const long long n = (long long)nx * ny * nz;
   const bool open = open_bc != 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    int z = (int)(i % nz);
-    long long r = i / nz;
-    int y = (int)(r % ny);
-    int x = (int)(r / ny);
+  for_each_cell(nx, ny, nz, [&](long long i, int x, int y, int z) {
     Cell<float> c[3];
 #pragma unroll
     for (int d = -1; d <= 1; ++d) {
@@ -748,7 +743,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(const float* __restrict__ sr
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v) dst[v * n + i] = o[v];
-  }
+  });
 }
 
 }  // namespace tf
@@ -1027,15 +1022,15 @@ int tf_evolve_along_axis(const float* W_in, float* W_out, int nx, int ny, int nz
   if ((flags & TF_FLAG_EXACT) && !(in_prim && out_prim))
     return set_error(TF_ERR_ARG, "the exact sweep works on primitive states only");
   cudaStream_t s = (cudaStream_t)stream;
-  int grid = elementwise_grid(n);
+  const RowLaunch rl = row_launch(nx, ny, nz);
   if (flags & TF_FLAG_EXACT) {
-    if (axis == 0) sweep_kernel<ExactPolicy<float>, 1><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
-    if (axis == 1) sweep_kernel<ExactPolicy<float>, 2><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
-    if (axis == 2) sweep_kernel<ExactPolicy<float>, 3><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
+    if (axis == 0) sweep_kernel<ExactPolicy<float>, 1><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
+    if (axis == 1) sweep_kernel<ExactPolicy<float>, 2><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
+    if (axis == 2) sweep_kernel<ExactPolicy<float>, 3><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
   } else {
-    if (axis == 0) sweep_kernel<FastPolicy, 1><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
-    if (axis == 1) sweep_kernel<FastPolicy, 2><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
-    if (axis == 2) sweep_kernel<FastPolicy, 3><<<grid, 256, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
+    if (axis == 0) sweep_kernel<FastPolicy, 1><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
+    if (axis == 1) sweep_kernel<FastPolicy, 2><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
+    if (axis == 2) sweep_kernel<FastPolicy, 3><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
   }
   return launch_check("sweep_kernel");
 }
