@@ -746,6 +746,69 @@ __global__ void __launch_bounds__(256) sweep_kernel(const float* __restrict__ sr
   });
 }
 
+// Per-axis sweep along x or y (VEL 1 or 2) that marches: a thread owns one
+// (other in-plane coordinate, z) column and walks a chunk of the sweep axis,
+// keeping the previous cell's quantities and the flux of the face behind it,
+// so each cell is loaded and derived once and each face is solved once.  The
+// operations on every face and cell are those of sweep_kernel, so the result
+// is the same bits.  z stays with sweep_kernel (a z march would not coalesce).
+template <class P, int VEL>
+__global__ void __launch_bounds__(256) march_sweep_kernel(const float* __restrict__ src,
+                                                          float* __restrict__ dst, int nx, int ny,
+                                                          int nz, int chunk, int open_bc,
+                                                          int in_prim, int out_prim,
+                                                          StepConsts<float> K) {
+  static_assert(VEL == 1 || VEL == 2, "x or y sweeps only");
+  const long long n = (long long)nx * ny * nz;
+  const bool open = open_bc != 0;
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  if (z >= nz) return;
+  const int o = blockIdx.y;                        // y for an x sweep, x for a y sweep
+  const int na = VEL == 1 ? nx : ny;               // length of the sweep axis
+  const int a0 = blockIdx.z * chunk, a_end = min(a0 + chunk, na);
+  const int zs = src_index(z, nz, open);
+  const int os = src_index(o, VEL == 1 ? ny : nx, open);
+  auto index = [&](int a) {  // linear index of cell a of this column
+    return VEL == 1 ? ((long long)a * ny + o) * nz + z : ((long long)o * ny + a) * nz + z;
+  };
+  auto derive_src = [&](int a, Cell<float>& c) {  // cell a read as the sweep reads it
+    const int as = src_index(a, na, open);
+    const long long j = VEL == 1 ? ((long long)as * ny + os) * nz + zs
+                                 : ((long long)os * ny + as) * nz + zs;
+    float w[5], st[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) w[v] = __ldg(src + v * n + j);
+    if (in_prim) P::to_state(w, st, K);
+    else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) st[v] = w[v];
+    }
+    P::template derive<VEL>(st, c, K);
+  };
+  Cell<float> prev, cur, next;
+  float flo[5], fhi[5];
+  derive_src(a0 - 1, prev);
+  derive_src(a0, cur);
+  P::hll(prev, cur, flo);
+  for (int a = a0; a < a_end; ++a) {
+    derive_src(a + 1, next);
+    P::hll(cur, next, fhi);
+    float st[5], out[5];
+    P::update(cur, flo, fhi, st, K);
+    if (out_prim) P::to_prim(st, out, K);
+    else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) out[v] = st[v];
+    }
+    const long long i = index(a);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) dst[v * n + i] = out[v];
+    cur = next;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) flo[v] = fhi[v];
+  }
+}
+
 }  // namespace tf
 
 using namespace tf;
@@ -1022,17 +1085,33 @@ int tf_evolve_along_axis(const float* W_in, float* W_out, int nx, int ny, int nz
   if ((flags & TF_FLAG_EXACT) && !(in_prim && out_prim))
     return set_error(TF_ERR_ARG, "the exact sweep works on primitive states only");
   cudaStream_t s = (cudaStream_t)stream;
-  const RowLaunch rl = row_launch(nx, ny, nz);
-  if (flags & TF_FLAG_EXACT) {
-    if (axis == 0) sweep_kernel<ExactPolicy<float>, 1><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
-    if (axis == 1) sweep_kernel<ExactPolicy<float>, 2><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
-    if (axis == 2) sweep_kernel<ExactPolicy<float>, 3><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
-  } else {
-    if (axis == 0) sweep_kernel<FastPolicy, 1><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
-    if (axis == 1) sweep_kernel<FastPolicy, 2><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
-    if (axis == 2) sweep_kernel<FastPolicy, 3><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
+  const bool exact = (flags & TF_FLAG_EXACT) != 0;
+  if (axis == 2) {
+    const RowLaunch rl = row_launch(nx, ny, nz);
+    if (exact) sweep_kernel<ExactPolicy<float>, 3><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, 1, 1, K);
+    else sweep_kernel<FastPolicy, 3><<<rl.blocks, rl.threads, 0, s>>>(W_in, W_out, nx, ny, nz, open, in_prim, out_prim, K);
+    return launch_check("sweep_kernel");
   }
-  return launch_check("sweep_kernel");
+  // x / y: march along the axis in chunks sized for ~8 waves of 256 threads
+  const int na = axis == 0 ? nx : ny, other = axis == 0 ? ny : nx;
+  const int threads = nz >= 256 ? 256 : ((nz + 31) / 32) * 32;
+  const long long zblocks = (nz + threads - 1) / threads;
+  if (other > 65535) return set_error(TF_ERR_ARG, "grid too large for the sweep launch");
+  const long long want = 8LL * sm_count() * (2048 / threads);
+  long long chunks = (want + zblocks * other - 1) / (zblocks * other);
+  const long long max_chunks = na / 4 > 0 ? na / 4 : 1;  // chunks of >= 4 cells
+  if (chunks > max_chunks) chunks = max_chunks;
+  if (chunks > 65535) chunks = 65535;
+  const int chunk = (int)((na + chunks - 1) / chunks);
+  const dim3 grid((unsigned)zblocks, (unsigned)other, (unsigned)((na + chunk - 1) / chunk));
+  if (exact) {
+    if (axis == 0) march_sweep_kernel<ExactPolicy<float>, 1><<<grid, threads, 0, s>>>(W_in, W_out, nx, ny, nz, chunk, open, 1, 1, K);
+    else march_sweep_kernel<ExactPolicy<float>, 2><<<grid, threads, 0, s>>>(W_in, W_out, nx, ny, nz, chunk, open, 1, 1, K);
+  } else {
+    if (axis == 0) march_sweep_kernel<FastPolicy, 1><<<grid, threads, 0, s>>>(W_in, W_out, nx, ny, nz, chunk, open, in_prim, out_prim, K);
+    else march_sweep_kernel<FastPolicy, 2><<<grid, threads, 0, s>>>(W_in, W_out, nx, ny, nz, chunk, open, in_prim, out_prim, K);
+  }
+  return launch_check("march_sweep_kernel");
 }
 
 }  // extern "C"
