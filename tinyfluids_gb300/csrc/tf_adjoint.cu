@@ -205,6 +205,70 @@ __global__ void __launch_bounds__(256) adjoint_sweep_kernel(const T* __restrict_
   });
 }
 
+// Adjoint of one periodic sweep along x or y (VEL 1 or 2) that marches: a
+// thread owns one (y or x, z) column and walks a chunk of the sweep axis,
+// carrying the previous cell's forward quantities and its partly accumulated
+// lam_in, so each cell's forward side is computed once and each face's VJP
+// once.  Every cell's lam_in receives the same additions in the same order
+// as in adjoint_sweep_kernel (its lam_out, then its left face, then its right
+// face), so the result is the same bits.
+template <typename T, int VEL>
+__global__ void __launch_bounds__(256) march_adjoint_kernel(const T* __restrict__ U,
+                                                            const T* __restrict__ lam_out,
+                                                            T* __restrict__ lam_in, AdjGeom G, T k,
+                                                            T g, int chunk) {
+  static_assert(VEL == 1 || VEL == 2, "x or y sweeps only");
+  const long long n = (long long)G.nx * G.ny * G.nz;
+  const T gm1 = g - T(1);
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  if (z >= G.nz) return;
+  const int o = blockIdx.y;  // y for an x sweep, x for a y sweep
+  const int na = VEL == 1 ? G.nx : G.ny;
+  const int a0 = blockIdx.z * chunk, a_end = min(a0 + chunk, na);
+  auto index = [&](int a) {
+    a = wrap_index(a, na);
+    return VEL == 1 ? ((long long)a * G.ny + o) * G.nz + z : ((long long)o * G.ny + a) * G.nz + z;
+  };
+  auto load = [&](int a, Side<T>& sd, T l[5]) {
+    const long long j = index(a);
+    T u[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      u[v] = U[v * n + j];
+      l[v] = lam_out[v * n + j];
+    }
+    side_forward<T, VEL>(u, g, gm1, sd);
+  };
+  Side<T> prev, cur, next;
+  T l_prev[5], l_cur[5], l_next[5], acc_cur[5], acc_next[5], gb[5], dummy[5];
+  load(a0 - 1, prev, l_prev);
+  load(a0, cur, l_cur);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    gb[v] = k * (l_cur[v] - l_prev[v]);  // face a0-1/2
+    acc_cur[v] = l_cur[v];
+    dummy[v] = T(0);
+  }
+  hll_vjp<T, VEL>(prev, cur, gb, g, gm1, dummy, acc_cur);
+  for (int a = a0; a < a_end; ++a) {
+    load(a + 1, next, l_next);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      gb[v] = k * (l_next[v] - l_cur[v]);  // face a+1/2
+      acc_next[v] = l_next[v];
+    }
+    hll_vjp<T, VEL>(cur, next, gb, g, gm1, acc_cur, acc_next);
+    const long long i = index(a);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      lam_in[v * n + i] = acc_cur[v];
+      acc_cur[v] = acc_next[v];
+      l_cur[v] = l_next[v];
+    }
+    cur = next;
+  }
+}
+
 // Forward sweep in conserved variables, for the FP64 finite-difference check
 // (float runs use the fast sweep kernel of tf_step.cu with conserved I/O).
 template <typename T, int VEL>
@@ -245,10 +309,25 @@ static int launch_adj(bool adjoint, const T* U, const T* lam_out, T* out, int nx
   T k = (T)(dt / dx), g = (T)gamma;
   if (sizeof(T) == 4) k = (T)((float)dt * (1.f / (float)dx));  // as the fast sweep: dt * (1/dx)
   if (adjoint) {
-    if (axis == 0) adjoint_sweep_kernel<T, 1><<<rl.blocks, rl.threads, 0, s>>>(U, lam_out, out, G, k, g);
-    if (axis == 1) adjoint_sweep_kernel<T, 2><<<rl.blocks, rl.threads, 0, s>>>(U, lam_out, out, G, k, g);
-    if (axis == 2) adjoint_sweep_kernel<T, 3><<<rl.blocks, rl.threads, 0, s>>>(U, lam_out, out, G, k, g);
-    return launch_check("adjoint_sweep_kernel");
+    if (axis == 2) {
+      adjoint_sweep_kernel<T, 3><<<rl.blocks, rl.threads, 0, s>>>(U, lam_out, out, G, k, g);
+      return launch_check("adjoint_sweep_kernel");
+    }
+    // x / y: march in chunks sized for ~8 waves of 256 threads
+    const int na = axis == 0 ? nx : ny, other = axis == 0 ? ny : nx;
+    const int threads = nz >= 256 ? 256 : ((nz + 31) / 32) * 32;
+    const long long zblocks = (nz + threads - 1) / threads;
+    if (other > 65535) return set_error(TF_ERR_ARG, "grid too large for the adjoint launch");
+    const long long want = 8LL * sm_count() * (2048 / threads);
+    long long chunks = (want + zblocks * other - 1) / (zblocks * other);
+    const long long max_chunks = na / 4 > 0 ? na / 4 : 1;
+    if (chunks > max_chunks) chunks = max_chunks;
+    if (chunks > 65535) chunks = 65535;
+    const int chunk = (int)((na + chunks - 1) / chunks);
+    const dim3 grid((unsigned)zblocks, (unsigned)other, (unsigned)((na + chunk - 1) / chunk));
+    if (axis == 0) march_adjoint_kernel<T, 1><<<grid, threads, 0, s>>>(U, lam_out, out, G, k, g, chunk);
+    else march_adjoint_kernel<T, 2><<<grid, threads, 0, s>>>(U, lam_out, out, G, k, g, chunk);
+    return launch_check("march_adjoint_kernel");
   }
   if (axis == 0) cons_sweep_kernel<T, 1><<<rl.blocks, rl.threads, 0, s>>>(U, out, G, k, g);
   if (axis == 1) cons_sweep_kernel<T, 2><<<rl.blocks, rl.threads, 0, s>>>(U, out, G, k, g);
