@@ -8,7 +8,7 @@ iterations (scaling_jax.py:70), so ``round(total / per_iteration)`` is the
 reference's iteration count for ``setup_ics(N, N//16)``, gamma=5/3,
 handle_boundaries=True (scaling_jax.py:86-93, 236).
 
-Usage: python tests/golden/make_golden.py /root/reference
+Usage: python tests/golden/make_golden.py <path of the reference checkout>
 """
 import json
 import os
@@ -41,4 +41,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the reference checkout>")
+    main(sys.argv[1])
