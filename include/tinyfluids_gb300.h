@@ -231,11 +231,20 @@ int tf_sweep_conserved_f64(const double *U, double *out, int nx, int ny, int nz,
  * fixed scratch array compiled into the library (about 5 MiB per GPU that
  * loads it, held until exit), so the caller passes only W_in and W_out, and
  * nothing is allocated.  Grids above TF_NOALLOC_MAX_CELLS cells are rejected
- * with TF_ERR_ARG.  The first call on a device looks up the scratch's device
- * address; make that first call before any stream capture.  All calls share
- * the one scratch array: calls that may overlap on the GPU (other streams,
- * other threads) race and must be serialised by the caller.  No counterpart
- * in the reference (it has no allocation control). */
+ * with TF_ERR_ARG, and so are states whose bytes overlap each other or the
+ * scratch.  The run uses tf_time_integration's default tile (16 rows).  The
+ * first call on a device looks up the scratch's device address and caches it
+ * for the life of the process; make that first call before any stream
+ * capture, and do not use the entry point across a cudaDeviceReset (which
+ * invalidates the address).  All calls share the one scratch array, which
+ * keeps the previous call's contents (each call re-initialises the control
+ * block it uses): calls that may overlap on the GPU (other streams, other
+ * threads) race and must be serialised by the caller.
+ * Errors found on the device (TF_ERR_NONFINITE, TF_ERR_TIMEOUT): a t_final run
+ * (max_steps < 0) checks the loop on the host and always reports them; a run
+ * of a known step count is asynchronous and reports them only when iters_host
+ * is non-NULL (the call then waits for the run).  No counterpart in the
+ * reference (it has no allocation control). */
 int tf_time_integration_noalloc(const float *W_in, float *W_out, int nx, int ny, int nz,
                                 float dx, float t_final, float gamma, float cfl, int max_steps,
                                 float fixed_dt, unsigned flags, int *iters_host, void *stream);

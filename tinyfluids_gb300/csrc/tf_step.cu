@@ -1135,7 +1135,9 @@ static __device__ __align__(256) unsigned char tf_noalloc_scratch[kNoallocBytes]
 
 // Device address of the scratch on the current device.  In host code the
 // array's name is only a host-side handle, so it is looked up once per device
-// (with that device current) and cached.
+// (with that device current) and cached for the life of the process; a
+// cudaDeviceReset unloads the module and invalidates the cached address, so
+// the entry point must not be used across one.
 constexpr int kNoallocMaxDevices = 64;
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_addr[kNoallocMaxDevices] = {};
@@ -1180,11 +1182,23 @@ extern "C" int tf_time_integration_noalloc(const float* W_in, float* W_out, int 
   TF_TRY(noalloc_scratch(&scratch));
   tf_ctl* ctl = (tf_ctl*)scratch;
   float* work = (float*)(scratch + kNoallocCtlBytes);
-  if (W_out == work || W_in == work) return set_error(TF_ERR_ARG, "states must not be the scratch");
+  // byte ranges of the two states and of the scratch must be disjoint
+  const uintptr_t state_bytes = (uintptr_t)(5 * n) * sizeof(float);
+  auto overlap = [](uintptr_t a, uintptr_t na, uintptr_t b, uintptr_t nb) {
+    return a < b + nb && b < a + na;
+  };
+  const uintptr_t in_p = (uintptr_t)W_in, out_p = (uintptr_t)W_out, sc_p = (uintptr_t)scratch;
+  if (overlap(in_p, state_bytes, out_p, state_bytes))
+    return set_error(TF_ERR_ARG, "W_in and W_out overlap");
+  if (overlap(in_p, state_bytes, sc_p, kNoallocBytes) ||
+      overlap(out_p, state_bytes, sc_p, kNoallocBytes))
+    return set_error(TF_ERR_ARG, "W_in / W_out overlap the library's allocation-free scratch");
 
   cudaStream_t s = (cudaStream_t)stream;
   const bool exact = (flags & TF_FLAG_EXACT) != 0;
-  int rows = 32, lx = 0;
+  // the tile of tf_time_integration's default (16 rows, heuristic chunk length)
+  int rows, lx, loader;
+  TF_TRY(resolve_tile(nullptr, &rows, &lx, &loader));
   // the control block keeps the previous call's contents: re-initialise all of it
   ctl_init_kernel<<<1, 1, 0, s>>>(ctl, t_final, cfl * dx, max_steps);
   maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W_in, n, gamma, ctl, exact ? 0 : 1);
@@ -1201,18 +1215,21 @@ extern "C" int tf_time_integration_noalloc(const float* W_in, float* W_out, int 
   a.ctl = ctl;
   a.fixed_dt = fixed_dt;
   if (max_steps >= 0) {
-    for (int i = 0; i < max_steps; ++i) TF_TRY(launch_fused(a, rows, exact, s));
+    for (int i = 0; i < max_steps; ++i) TF_TRY(launch_fused(a, rows, exact, s, loader));
   } else {
     tf_ctl h;  // host copy of the loop state (pageable, on the stack)
     int chunk = 8;
     long long launched = 0;
     float t_prev = -1.f;
     for (;;) {
-      for (int i = 0; i < chunk; ++i) TF_TRY(launch_fused(a, rows, exact, s));
+      for (int i = 0; i < chunk; ++i) TF_TRY(launch_fused(a, rows, exact, s, loader));
       launched += chunk;
       TF_TRY(cuda_check(cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, s),
                         "cudaMemcpyAsync(ctl)"));
       TF_TRY(cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
+      if (h.status != TF_OK)  // reported whether or not iters_host is given
+        return set_error(h.status, "device reported %s after %d steps",
+                         tf_status_string(h.status), h.iter);
       if (!h.active) break;
       if (h.t == t_prev)
         return set_error(TF_ERR_NONFINITE, "time stalled at t=%g", (double)h.t);
