@@ -144,6 +144,13 @@ int tf_debug_checked(void);
 int tf_debug_set_graph_loop_cap(int cap);
 int tf_debug_reset(int *write_counts, long long ncells);
 long long tf_debug_oob_count(void);
+/* The adjoint sweep of tf_adjoint_sweep computed one thread per cell with
+ * both faces' VJPs recomputed (the form the marching x / y adjoint kernels
+ * replace), on any axis: lets a test check that the marching kernels give
+ * the same bits.  No reference counterpart. */
+int tf_debug_adjoint_sweep_per_cell(const float *U, const float *lam_out, float *lam_in, int nx,
+                                    int ny, int nz, float dx, float dt, float gamma, int axis,
+                                    void *stream);
 
 /* time_integration.py:94-128 (plain branch): while t < t_final: dt = CFL dt;
  * W = step(W, dt); t += dt; iter += 1.  max_steps >= 0 also bounds the loop

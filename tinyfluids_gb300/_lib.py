@@ -63,6 +63,8 @@ SIGNATURES = {
     "tf_debug_set_graph_loop_cap": (c_int, [c_int]),
     "tf_debug_reset": (c_int, [vp, c_ll]),
     "tf_debug_oob_count": (c_ll, []),
+    "tf_debug_adjoint_sweep_per_cell": (c_int, [vp, vp, vp, c_int, c_int, c_int, c_float,
+                                                c_float, c_float, c_int, vp]),
     "tf_time_integration": (c_int, [vp, vp, vp, vp, c_int, c_int, c_int, c_float, c_float,
                                     c_float, c_float, c_int, c_float, c_uint, vp, vp, vp]),
     "tf_evolve_along_axis": (c_int, [vp, vp, c_int, c_int, c_int, c_float, c_float, vp,

@@ -297,7 +297,8 @@ __global__ void __launch_bounds__(256) cons_sweep_kernel(const T* __restrict__ U
 
 template <typename T>
 static int launch_adj(bool adjoint, const T* U, const T* lam_out, T* out, int nx, int ny, int nz,
-                      double dx, double dt, double gamma, int axis, cudaStream_t s) {
+                      double dx, double dt, double gamma, int axis, cudaStream_t s,
+                      bool per_cell = false) {
   if (!U || !out || (adjoint && !lam_out)) return set_error(TF_ERR_ARG, "null pointer");
   if (out == U || (adjoint && out == lam_out)) return set_error(TF_ERR_ARG, "output aliases input");
   if (nx < 1 || ny < 1 || nz < 1) return set_error(TF_ERR_ARG, "grid dims must be >= 1");
@@ -309,8 +310,10 @@ static int launch_adj(bool adjoint, const T* U, const T* lam_out, T* out, int nx
   T k = (T)(dt / dx), g = (T)gamma;
   if (sizeof(T) == 4) k = (T)((float)dt * (1.f / (float)dx));  // as the fast sweep: dt * (1/dx)
   if (adjoint) {
-    if (axis == 2) {
-      adjoint_sweep_kernel<T, 3><<<rl.blocks, rl.threads, 0, s>>>(U, lam_out, out, G, k, g);
+    if (axis == 2 || per_cell) {
+      if (axis == 0) adjoint_sweep_kernel<T, 1><<<rl.blocks, rl.threads, 0, s>>>(U, lam_out, out, G, k, g);
+      if (axis == 1) adjoint_sweep_kernel<T, 2><<<rl.blocks, rl.threads, 0, s>>>(U, lam_out, out, G, k, g);
+      if (axis == 2) adjoint_sweep_kernel<T, 3><<<rl.blocks, rl.threads, 0, s>>>(U, lam_out, out, G, k, g);
       return launch_check("adjoint_sweep_kernel");
     }
     // x / y: march in chunks sized for ~8 waves of 256 threads
@@ -345,6 +348,13 @@ int tf_adjoint_sweep(const float* U, const float* lam_out, float* lam_in, int nx
                      float dx, float dt, float gamma, int axis, void* stream) {
   return launch_adj<float>(true, U, lam_out, lam_in, nx, ny, nz, dx, dt, gamma, axis,
                            (cudaStream_t)stream);
+}
+
+int tf_debug_adjoint_sweep_per_cell(const float* U, const float* lam_out, float* lam_in, int nx,
+                                    int ny, int nz, float dx, float dt, float gamma, int axis,
+                                    void* stream) {
+  return launch_adj<float>(true, U, lam_out, lam_in, nx, ny, nz, dx, dt, gamma, axis,
+                           (cudaStream_t)stream, true);
 }
 
 int tf_adjoint_sweep_f64(const double* U, const double* lam_out, double* lam_in, int nx, int ny,
