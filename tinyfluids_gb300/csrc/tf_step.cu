@@ -297,38 +297,37 @@ __global__ void __launch_bounds__(256) diagnostics_kernel(const float* __restric
 // fused step
 // ---------------------------------------------------------------------------
 struct FusedArgs {
-  const float* src0;  // input state (iteration 0 in loop mode)
-  float* buf[2];      // fixed mode: buf[1] = output; loop mode: ping-pong
+  // The buffers of this launch.  A run loop passes, per launch, the source
+  // and destination of that step (the ping-pong parity is known on the host),
+  // so the kernel's addresses derive from launch arguments only and are the
+  // same for every thread of a CTA.
+  const float* src;
+  float* dst;
   FusedGeom geo;
   float gamma, inv_dx, gm1, igm1;
   float dt_host;
   const float* dt_dev;
   float fixed_dt;  // loop mode: > 0 replaces ctl->dt
   tf_ctl* ctl;     // fixed mode: optional; loop mode: required
-  int loop;        // 1: predicated loop step (parity buffers, dt from ctl)
+  int loop;        // 1: a step of a run loop (predicated on ctl->active, dt from ctl)
   double* totals;  // diagnostics instantiation: conserved totals (zeroed before)
   DiagArgs diag;   // diagnostics instantiation: optional slice
   int conserved_io;  // fast policy on conserved input and output (16-row tiles)
 };
 
-template <class P, int NWP, bool DIAG = false>
-__global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_kernel(FusedArgs a) {
-  __shared__ FusedSmem<NWP> sm;
-  __shared__ double dred[DIAG ? NWP * 5 : 1];
-  const float* src;
-  float* dst;
-  float dt;
+// dt of a launch: a loop step reads the loop's dt (or its fixed dt) and runs
+// only while the loop is active; a single step takes the caller's dt.
+__device__ __forceinline__ bool launch_dt(const FusedArgs& a, float* dt) {
   if (a.loop) {
-    if (!ld_volatile(&a.ctl->active)) return;
-    int iter = ld_volatile(&a.ctl->iter);
-    src = iter == 0 ? a.src0 : ((iter & 1) ? a.buf[1] : a.buf[0]);
-    dst = (iter & 1) ? a.buf[0] : a.buf[1];
-    dt = a.fixed_dt > 0.f ? a.fixed_dt : ld_volatile(&a.ctl->dt);
+    if (!ld_volatile(&a.ctl->active)) return false;
+    *dt = a.fixed_dt > 0.f ? a.fixed_dt : ld_volatile(&a.ctl->dt);
   } else {
-    src = a.src0;
-    dst = a.buf[1];
-    dt = a.dt_dev ? *a.dt_dev : a.dt_host;
+    *dt = a.dt_dev ? *a.dt_dev : a.dt_host;
   }
+  return true;
+}
+
+__device__ __forceinline__ StepConsts<float> launch_consts(const FusedArgs& a, float dt) {
   StepConsts<float> K;
   K.g = a.gamma;
   K.gm1 = a.gm1;
@@ -336,9 +335,19 @@ __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_ker
   K.inv_dx = a.inv_dx;
   K.dt = dt;
   K.k = dt * a.inv_dx;
+  return K;
+}
+
+template <class P, int NWP, bool DIAG = false>
+__global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_kernel(FusedArgs a) {
+  __shared__ FusedSmem<NWP> sm;
+  __shared__ double dred[DIAG ? NWP * 5 : 1];
+  float dt;
+  if (!launch_dt(a, &dt)) return;
+  const StepConsts<float> K = launch_consts(a, dt);
   CSum acc[5];
-  float m = fused_tile<P, NWP, false, DIAG>(src, dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z,
-                                            K, sm, a.diag, acc);
+  float m = fused_tile<P, NWP, false, DIAG>(a.src, a.dst, a.geo, blockIdx.x, blockIdx.y,
+                                            blockIdx.z, K, sm, a.diag, acc);
   if constexpr (DIAG) block_add_totals(acc, dred, a.totals);
   if (a.ctl) {
     float bm = block_max(m, sm.red);
@@ -347,46 +356,22 @@ __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_ker
   }
 }
 
-// The fused step with TMA-staged planes (fused_tile_tma).  The three tensor
-// maps describe src0, buf[0] and buf[1]; the loop form picks the one of the
-// current source like fused_step_kernel picks the pointer.
+// The fused step with TMA-staged planes (fused_tile_tma); the tensor map
+// describes a.src.
 template <class P, int NWP>
 __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP))
-    fused_step_tma_kernel(FusedArgs a, const __grid_constant__ CUtensorMap tm_src0,
-                          const __grid_constant__ CUtensorMap tm_b0,
-                          const __grid_constant__ CUtensorMap tm_b1) {
+    fused_step_tma_kernel(FusedArgs a, const __grid_constant__ CUtensorMap tm_src) {
   __shared__ FusedSmem<NWP> sm;
   __shared__ __align__(8) unsigned long long bars[kStages];
   extern __shared__ unsigned char dyn_smem[];
   float* stages = reinterpret_cast<float*>(
       (reinterpret_cast<uintptr_t>(dyn_smem) + 127) & ~static_cast<uintptr_t>(127));
-  const float* src;
-  float* dst;
-  const CUtensorMap* tm;
   float dt;
-  if (a.loop) {
-    if (!ld_volatile(&a.ctl->active)) return;
-    int iter = ld_volatile(&a.ctl->iter);
-    src = iter == 0 ? a.src0 : ((iter & 1) ? a.buf[1] : a.buf[0]);
-    tm = iter == 0 ? &tm_src0 : ((iter & 1) ? &tm_b1 : &tm_b0);
-    dst = (iter & 1) ? a.buf[0] : a.buf[1];
-    dt = a.fixed_dt > 0.f ? a.fixed_dt : ld_volatile(&a.ctl->dt);
-  } else {
-    src = a.src0;
-    tm = &tm_src0;
-    dst = a.buf[1];
-    dt = a.dt_dev ? *a.dt_dev : a.dt_host;
-  }
-  StepConsts<float> K;
-  K.g = a.gamma;
-  K.gm1 = a.gm1;
-  K.igm1 = a.igm1;
-  K.inv_dx = a.inv_dx;
-  K.dt = dt;
-  K.k = dt * a.inv_dx;
+  if (!launch_dt(a, &dt)) return;
+  const StepConsts<float> K = launch_consts(a, dt);
   bool timed_out = false;
-  float m = fused_tile_tma<P, NWP>(src, dst, tm, a.geo, blockIdx.x, blockIdx.y, blockIdx.z, K,
-                                   sm, stages, bars, &timed_out);
+  float m = fused_tile_tma<P, NWP>(a.src, a.dst, &tm_src, a.geo, blockIdx.x, blockIdx.y,
+                                   blockIdx.z, K, sm, stages, bars, &timed_out);
   if (a.ctl) {
     float bm = block_max(m, sm.red);
     if (threadIdx.x == 0) {
@@ -435,9 +420,7 @@ static bool make_state_tmap(CUtensorMap* m, const float* base, int nx, int ny, i
 static bool tma_usable(const FusedArgs& a, int rows) {
   if (rows != 8 && rows != 16 && rows != 32) return false;
   if (a.geo.nz % 4 != 0) return false;  // tensor strides must be multiples of 16 bytes
-  const float* ptrs[3] = {a.src0, a.buf[0], a.buf[1]};
-  for (const float* p : ptrs)
-    if (p && (reinterpret_cast<uintptr_t>(p) & 15)) return false;
+  if ((reinterpret_cast<uintptr_t>(a.src) | reinterpret_cast<uintptr_t>(a.dst)) & 15) return false;
   return encode_tiled() != nullptr;
 }
 
@@ -514,17 +497,15 @@ static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx, int* loa
 }
 
 template <int NWP>
-static int launch_tma(const FusedArgs& a, dim3 grid, const CUtensorMap* tm, bool exact,
+static int launch_tma(const FusedArgs& a, dim3 grid, const CUtensorMap& tm, bool exact,
                       cudaStream_t s) {
-  {
-    const size_t smem = tma_smem_bytes(NWP) + 128;
-    auto k = exact ? fused_step_tma_kernel<ExactPair, NWP> : fused_step_tma_kernel<FastPair, NWP>;
-    TF_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem),
-                      "cudaFuncSetAttribute"));
-    k<<<grid, NWP * 32, smem, s>>>(a, tm[0], tm[1], tm[2]);
-    return TF_OK;
-  }
+  const size_t smem = tma_smem_bytes(NWP) + 128;
+  auto k = exact ? fused_step_tma_kernel<ExactPair, NWP> : fused_step_tma_kernel<FastPair, NWP>;
+  TF_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem),
+                    "cudaFuncSetAttribute"));
+  k<<<grid, NWP * 32, smem, s>>>(a, tm);
+  return TF_OK;
 }
 
 // Launches one fused step.  loader: 0 auto, 1 per-thread loads, 2 TMA-staged
@@ -536,12 +517,8 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
     return set_error(TF_ERR_ARG, "grid too large for the tile grid");
   dim3 grid(a.geo.tiles_z, a.geo.tiles_y, a.geo.tiles_x);
   if (loader == 2 && tma_usable(a, rows)) {
-    CUtensorMap tm[3];
-    const float* bases[3] = {a.src0, a.buf[0] ? a.buf[0] : a.src0, a.buf[1]};
-    bool ok = true;
-    for (int i = 0; i < 3 && ok; ++i)
-      ok = make_state_tmap(&tm[i], bases[i], a.geo.nx, a.geo.ny, a.geo.nz, rows);
-    if (ok) {
+    CUtensorMap tm;
+    if (make_state_tmap(&tm, a.src, a.geo.nx, a.geo.ny, a.geo.nz, rows)) {
       TF_DISPATCH_ROWS(rows, NWP, TF_TRY((launch_tma<NWP>(a, grid, tm, exact, s))));
       return launch_check("fused_step_tma_kernel");
     }
@@ -567,15 +544,34 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
   return launch_check("fused_step_kernel");
 }
 
-// The t_final loop as a CUDA graph: a while node whose body is {one
-// predicated fused step, loop_cond_kernel}, entered after one condition
-// evaluation.  The kernel arguments bake in the buffers and scalars, so
-// executable graphs are cached by (device, arguments, tile): a repeated call
-// on the same buffers launches the cached graph.  An evicted graph is
-// destroyed at once; CUDA frees it after any in-flight launch completes.
+// The buffers of a run loop.  Step i (1-based) reads `in` for i == 1, else
+// buf[(i - 1) & 1], and writes buf[i & 1]; after n steps the state is in
+// `in` (n == 0) or buf[n & 1].
+struct LoopBufs {
+  const float* in;
+  float* buf[2];
+};
+
+static FusedArgs step_args(FusedArgs a, const LoopBufs& b, long long i) {
+  a.src = i == 1 ? b.in : b.buf[(i - 1) & 1];
+  a.dst = b.buf[i & 1];
+  return a;
+}
+
+// The t_final loop as a CUDA graph: {condition, step 1, condition} and then a
+// while node whose body is {even step, condition, odd step, condition}, so
+// every step launch carries its own buffers.  Each step is predicated on the
+// loop condition the previous step's last CTA (or the condition kernel) left
+// in the control block, so a loop that ends after an odd step skips the
+// body's second step.  The kernel arguments bake in the buffers and scalars,
+// so executable graphs are cached by (device, arguments, buffers, tile): a
+// repeated call on the same buffers launches the cached graph.  An evicted
+// graph is destroyed at once; CUDA frees it after any in-flight launch
+// completes.
 struct GraphKey {
   int device, rows, exact, cap;
-  FusedArgs a;  // zero-initialised, so padding compares equal
+  FusedArgs a;  // with src / dst cleared; zero-initialised, so padding compares equal
+  LoopBufs b;
 };
 struct GraphEntry {
   GraphKey key;
@@ -585,10 +581,11 @@ static std::mutex g_graph_mu;
 static std::vector<GraphEntry> g_graphs;  // most recently used last
 constexpr size_t kGraphCacheSize = 8;
 
-static int build_graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, int cap,
-                            cudaGraphExec_t* out);
+static int build_graph_loop(const FusedArgs& a, const LoopBufs& b, int rows, bool exact,
+                            tf_ctl* ctl, int cap, cudaGraphExec_t* out);
 
-static int graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, cudaStream_t s) {
+static int graph_loop(const FusedArgs& a, const LoopBufs& b, int rows, bool exact, tf_ctl* ctl,
+                      cudaStream_t s) {
   GraphKey k;
   memset(&k, 0, sizeof k);
   TF_TRY(cuda_check(cudaGetDevice(&k.device), "cudaGetDevice"));
@@ -596,6 +593,9 @@ static int graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, cud
   k.exact = exact ? 1 : 0;
   k.cap = g_graph_loop_cap.load();
   k.a = a;
+  k.a.src = nullptr;
+  k.a.dst = nullptr;
+  k.b = b;
   std::lock_guard<std::mutex> lk(g_graph_mu);
   for (size_t i = 0; i < g_graphs.size(); ++i) {
     if (memcmp(&g_graphs[i].key, &k, sizeof k) == 0) {
@@ -606,7 +606,7 @@ static int graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, cud
     }
   }
   cudaGraphExec_t exec = nullptr;
-  TF_TRY(build_graph_loop(a, rows, exact, ctl, k.cap, &exec));
+  TF_TRY(build_graph_loop(a, b, rows, exact, ctl, k.cap, &exec));
   int st = cuda_check(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
   if (st != TF_OK) {
     cudaGraphExecDestroy(exec);
@@ -620,60 +620,88 @@ static int graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, cud
   return TF_OK;
 }
 
-static int build_graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ctl, int cap,
-                            cudaGraphExec_t* out) {
-  cudaGraph_t g = nullptr, body = nullptr;
+static int build_graph_loop(const FusedArgs& a, const LoopBufs& b, int rows, bool exact,
+                            tf_ctl* ctl, int cap, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t cs = nullptr;
   int st = TF_OK;
+  bool capturing = false;
   auto fail = [&](cudaError_t e, const char* what) {
     if (st == TF_OK && e != cudaSuccess) st = cuda_check(e, what);
     return st != TF_OK;
+  };
+  auto end_capture = [&]() {
+    cudaGraph_t captured = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(cs, &captured);
+    capturing = false;
+    return ce;
   };
   do {
     if (fail(cudaGraphCreate(&g, 0), "cudaGraphCreate")) break;
     cudaGraphConditionalHandle h;
     if (fail(cudaGraphConditionalHandleCreate(&h, g, 0, 0), "cudaGraphConditionalHandleCreate"))
       break;
-    // entry: evaluate the condition once (t_final may already be reached)
-    cudaGraphNode_t entry;
-    cudaKernelNodeParams kp;
-    memset(&kp, 0, sizeof kp);
-    void* cargs[3] = {(void*)&ctl, (void*)&h, (void*)&cap};
-    kp.func = (void*)loop_cond_kernel;
-    kp.gridDim = dim3(1);
-    kp.blockDim = dim3(1);
-    kp.kernelParams = cargs;
-    if (fail(cudaGraphAddKernelNode(&entry, g, nullptr, 0, &kp), "cudaGraphAddKernelNode"))
+    if (fail(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate")) break;
+    // prologue: condition (t_final may already be reached), step 1, condition
+    if (fail(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal),
+             "cudaStreamBeginCaptureToGraph"))
+      break;
+    capturing = true;
+    loop_cond_kernel<<<1, 1, 0, cs>>>(ctl, h, cap);
+    int lst = launch_check("loop_cond_kernel");
+    if (lst == TF_OK) lst = launch_fused(step_args(a, b, 1), rows, exact, cs, 1);
+    if (lst == TF_OK) {
+      loop_cond_kernel<<<1, 1, 0, cs>>>(ctl, h, cap);
+      lst = launch_check("loop_cond_kernel");
+    }
+    if (lst != TF_OK) {
+      st = lst;
+      break;
+    }
+    // the while node after the prologue
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    if (fail(cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &ndeps),
+             "cudaStreamGetCaptureInfo"))
       break;
     cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};  // other members zero
     np.conditional.handle = h;
     np.conditional.type = cudaGraphCondTypeWhile;
     np.conditional.size = 1;
     cudaGraphNode_t loop;
-    if (fail(cudaGraphAddNode(&loop, g, &entry, nullptr, 1, &np), "cudaGraphAddNode(while)"))
+    if (fail(cudaGraphAddNode(&loop, cg, deps, nullptr, ndeps, &np), "cudaGraphAddNode(while)"))
       break;
-    body = np.conditional.phGraph_out[0];
-    // the body: capture a step and the condition into the while node's graph
-    if (fail(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate")) break;
+    if (fail(cudaStreamUpdateCaptureDependencies(cs, &loop, nullptr, 1,
+                                                 cudaStreamSetCaptureDependencies),
+             "cudaStreamUpdateCaptureDependencies"))
+      break;
+    if (fail(end_capture(), "cudaStreamEndCapture")) break;
+    // the body: steps 2k and 2k + 1, each followed by the condition
+    cudaGraph_t body = np.conditional.phGraph_out[0];
     if (fail(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
                                            cudaStreamCaptureModeThreadLocal),
-             "cudaStreamBeginCaptureToGraph"))
+             "cudaStreamBeginCaptureToGraph(body)"))
       break;
-    int lst = launch_fused(a, rows, exact, cs, 1);
-    if (lst == TF_OK) {
-      loop_cond_kernel<<<1, 1, 0, cs>>>(ctl, h, cap);
-      lst = launch_check("loop_cond_kernel");
+    capturing = true;
+    for (int i = 2; i <= 3 && lst == TF_OK; ++i) {
+      lst = launch_fused(step_args(a, b, i), rows, exact, cs, 1);
+      if (lst == TF_OK) {
+        loop_cond_kernel<<<1, 1, 0, cs>>>(ctl, h, cap);
+        lst = launch_check("loop_cond_kernel");
+      }
     }
-    cudaGraph_t captured = nullptr;
-    cudaError_t ce = cudaStreamEndCapture(cs, &captured);
     if (lst != TF_OK) {
       st = lst;
       break;
     }
-    if (fail(ce, "cudaStreamEndCapture")) break;
+    if (fail(end_capture(), "cudaStreamEndCapture(body)")) break;
     if (fail(cudaGraphInstantiate(&exec, g, 0), "cudaGraphInstantiate")) break;
   } while (false);
+  if (capturing) end_capture();
   if (cs) cudaStreamDestroy(cs);
   if (g) cudaGraphDestroy(g);
   if (st != TF_OK && exec) {
@@ -684,13 +712,12 @@ static int build_graph_loop(const FusedArgs& a, int rows, bool exact, tf_ctl* ct
   return st;
 }
 
-static FusedArgs make_fused_args(const float* src, float* b0, float* b1, const FusedGeom& geo,
-                                 float dx, float gamma) {
+static FusedArgs make_fused_args(const float* src, float* dst, const FusedGeom& geo, float dx,
+                                 float gamma) {
   FusedArgs a;
   memset(&a, 0, sizeof a);
-  a.src0 = src;
-  a.buf[0] = b0;
-  a.buf[1] = b1;
+  a.src = src;
+  a.dst = dst;
   a.geo = geo;
   StepConsts<float> k = make_consts<float>(gamma, dx, 0.f);
   a.gamma = k.g;
@@ -881,7 +908,7 @@ int tf_evolve_state(const float* W_in, float* W_out, int nx, int ny, int nz, flo
   int rows, lx, loader;
   TF_TRY(resolve_tile(tile, &rows, &lx, &loader));
   FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
-  FusedArgs a = make_fused_args(W_in, nullptr, W_out, geo, dx, gamma);
+  FusedArgs a = make_fused_args(W_in, W_out, geo, dx, gamma);
   a.dt_host = dt_host;
   a.dt_dev = dt_dev;
   a.loop = 0;
@@ -910,7 +937,7 @@ int tf_evolve_state_diag(const float* W_in, float* W_out, int nx, int ny, int nz
   int rows, lx, loader;
   TF_TRY(resolve_tile(tile, &rows, &lx, &loader));
   FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
-  FusedArgs a = make_fused_args(W_in, nullptr, W_out, geo, dx, gamma);
+  FusedArgs a = make_fused_args(W_in, W_out, geo, dx, gamma);
   a.dt_host = dt_host;
   a.dt_dev = dt_dev;
   a.loop = 0;
@@ -1008,16 +1035,18 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
     b0 = W_out;
     b1 = work;
   }
-  FusedArgs a = make_fused_args(W_in, b0, b1, geo, dx, gamma);
+  FusedArgs a = make_fused_args(W_in, nullptr, geo, dx, gamma);
   a.loop = 1;
   a.ctl = ctl;
   a.fixed_dt = fixed_dt;
+  const LoopBufs bufs{W_in, {b0, b1}};
 
   if (max_steps >= 0) {
     // step count known: enqueue exactly that many predicated steps
-    for (int i = 0; i < max_steps; ++i) TF_TRY(launch_fused(a, rows, exact, s, loader));
+    for (int i = 1; i <= max_steps; ++i)
+      TF_TRY(launch_fused(step_args(a, bufs, i), rows, exact, s, loader));
   } else if (!(flags & TF_FLAG_HOST_LOOP)) {
-    TF_TRY(graph_loop(a, rows, exact, ctl, s));
+    TF_TRY(graph_loop(a, bufs, rows, exact, ctl, s));
   } else {
     // run to t_final: chunks of predicated steps, one host check per chunk
     static thread_local tf_ctl* pinned = nullptr;
@@ -1026,7 +1055,8 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
     long long launched = 0;
     float t_prev = -1.f;
     for (;;) {
-      for (int i = 0; i < chunk; ++i) TF_TRY(launch_fused(a, rows, exact, s, loader));
+      for (int i = 1; i <= chunk; ++i)
+        TF_TRY(launch_fused(step_args(a, bufs, launched + i), rows, exact, s, loader));
       launched += chunk;
       TF_TRY(cuda_check(cudaMemcpyAsync(pinned, ctl, sizeof(tf_ctl), cudaMemcpyDeviceToHost, s),
                         "cudaMemcpyAsync(ctl)"));
@@ -1210,19 +1240,22 @@ extern "C" int tf_time_integration_noalloc(const float* W_in, float* W_out, int 
     b0 = W_out;
     b1 = work;
   }
-  FusedArgs a = make_fused_args(W_in, b0, b1, geo, dx, gamma);
+  FusedArgs a = make_fused_args(W_in, nullptr, geo, dx, gamma);
   a.loop = 1;
   a.ctl = ctl;
   a.fixed_dt = fixed_dt;
+  const LoopBufs bufs{W_in, {b0, b1}};
   if (max_steps >= 0) {
-    for (int i = 0; i < max_steps; ++i) TF_TRY(launch_fused(a, rows, exact, s, loader));
+    for (int i = 1; i <= max_steps; ++i)
+      TF_TRY(launch_fused(step_args(a, bufs, i), rows, exact, s, loader));
   } else {
     tf_ctl h;  // host copy of the loop state (pageable, on the stack)
     int chunk = 8;
     long long launched = 0;
     float t_prev = -1.f;
     for (;;) {
-      for (int i = 0; i < chunk; ++i) TF_TRY(launch_fused(a, rows, exact, s, loader));
+      for (int i = 1; i <= chunk; ++i)
+        TF_TRY(launch_fused(step_args(a, bufs, launched + i), rows, exact, s, loader));
       launched += chunk;
       TF_TRY(cuda_check(cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, s),
                         "cudaMemcpyAsync(ctl)"));
