@@ -172,7 +172,7 @@ __device__ __forceinline__ void tile_coords(const FusedGeom& g, int t, int& tz, 
 
 // One step of every active instance: one CTA per (instance, tile).
 template <class P, int NWP>
-__global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) batch_step_kernel(const BatchInst* __restrict__ inst,
+__global__ void TF_FUSED_BOUNDS(NWP) batch_step_kernel(const BatchInst* __restrict__ inst,
                                                                 const int* __restrict__ tile_prefix,
                                                                 int count) {
   __shared__ FusedSmem<NWP> sm;
@@ -201,7 +201,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 // All steps of all instances in one launch (see the file comment).
 template <class P, int NWP>
-__global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP))
+__global__ void TF_FUSED_BOUNDS(NWP)
     batch_persistent_kernel(BatchHeader* hdr, const BatchInst* __restrict__ inst,
                             const int* __restrict__ tile_prefix, int count, int tiles_per_step,
                             int step_base, int steps, unsigned long long wait_limit) {
@@ -323,7 +323,7 @@ int tf_batch_prepare(const tf_instance* inst, int count, const tf_batch_config* 
   plan.count = count;
   if (cfg) {
     if (!valid_tile_rows(cfg->rows))
-      return set_error(TF_ERR_ARG, "batch rows must be 8, 16 or 32 (got %d)", cfg->rows);
+      return set_error(TF_ERR_ARG, "batch rows must be 8, 16, 18 or 32 (got %d)", cfg->rows);
     plan.rows = cfg->rows;
     plan.exact = cfg->exact ? 1 : 0;
     plan.persistent = cfg->persistent ? 1 : 0;

@@ -339,7 +339,7 @@ __device__ __forceinline__ StepConsts<float> launch_consts(const FusedArgs& a, f
 }
 
 template <class P, int NWP, bool DIAG = false>
-__global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_kernel(FusedArgs a) {
+__global__ void TF_FUSED_BOUNDS(NWP) fused_step_kernel(FusedArgs a) {
   __shared__ FusedSmem<NWP> sm;
   __shared__ double dred[DIAG ? NWP * 5 : 1];
   float dt;
@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP)) fused_step_ker
 // The fused step with TMA-staged planes (fused_tile_tma); the tensor map
 // describes a.src.
 template <class P, int NWP>
-__global__ void __launch_bounds__(NWP * 32, min_ctas_per_sm(NWP))
+__global__ void TF_FUSED_BOUNDS(NWP)
     fused_step_tma_kernel(FusedArgs a, const __grid_constant__ CUtensorMap tm_src) {
   __shared__ FusedSmem<NWP> sm;
   __shared__ __align__(8) unsigned long long bars[kStages];
@@ -485,7 +485,7 @@ static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx, int* loa
   *loader = 0;
   if (tile) {
     if (!valid_tile_rows(tile->rows))
-      return set_error(TF_ERR_ARG, "tile rows must be 8, 16 or 32 (got %d)", tile->rows);
+      return set_error(TF_ERR_ARG, "tile rows must be 8, 16, 18 or 32 (got %d)", tile->rows);
     *rows = tile->rows;
     *lx = tile->lx;
     if (*lx < 0) return set_error(TF_ERR_ARG, "tile lx must be >= 0");
