@@ -56,6 +56,11 @@ def parse():
     p.add_argument("--instances", type=int, default=256)
     p.add_argument("--requests", type=int, default=120)
     p.add_argument("--rates", default="10,50,100,200,500")
+    p.add_argument("--serve-rate", type=float, default=200.0,
+                   help="arrival rate of the serving part of the default line")
+    p.add_argument("--serve-requests", type=int, default=300)
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the serving and batching parts of the default line")
     return p.parse_args()
 
 
@@ -145,7 +150,8 @@ class ClockSampler:
 
 def cpu_baseline(n, seconds_budget, steps_cap):
     """The C restatement of the reference step (all host threads) on an n^3
-    shear layer; times up to steps_cap steps, bounded by the time budget."""
+    shear layer; times up to steps_cap steps, bounded by the time budget.
+    The returned dict's "steps" is the number of steps timed."""
     import numpy as np
     from oracle import build as ob
     from oracle import fluid_c
@@ -163,20 +169,23 @@ def cpu_baseline(n, seconds_budget, steps_cap):
     el = time.perf_counter() - t0
     del np
     return {"value": n ** 3 * k / el / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{k} CFL steps of the {n}^3 shear layer (after 1 warm-up step), "
-                      f"C restatement of fluid.py/time_integration.py, {threads} OpenMP threads"}
+            "steps": k, "seconds": el,
+            "sample": f"{k} CFL steps of the {n}^3 shear layer timed (after 1 untimed warm-up "
+                      f"step), C restatement of fluid.py/time_integration.py, "
+                      f"{threads} OpenMP threads"}
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    budget = min(args.cpu_sample_seconds, 60.0)
-    cb = cpu_baseline(args.n, budget, max(1, args.steps))
+    # every requested step is timed unless that would take more than ~90 s
+    cb = cpu_baseline(args.n, 90.0, max(1, args.steps))
     line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "n_gpus": args.gpus, "steps": cb["steps"], "warmup": 1,
+            "steps_requested": args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "ms_per_step": 1e3 * args.n ** 3 / (cb["value"] * 1e9),
+            "data": "synthetic", "ms_per_step": 1e3 * cb["seconds"] / cb["steps"],
             "config": {"workload": f"shear layer {args.n}^3, gamma=5/3, CFL 0.4, periodic",
                        "instances": 1, "parallelism": "cpu"},
             "cpu_baseline": cb,
@@ -317,8 +326,16 @@ def run_gpu(args):
         "gpu_launches": K + 3,
         "clocks": clk,
     }
-    if not args.no_cpu_baseline and world == 1 or (not args.no_cpu_baseline and rank == 0):
-        line["cpu_baseline"] = cpu_baseline(min(n, 512), args.cpu_sample_seconds, 5)
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(min(n, 512), args.cpu_sample_seconds, K)
+    if world == 1 and not args.no_extras:
+        # the other two parts of the headline metric, measured on the same GPU
+        # after the timed region: served solves/s with p50/p99 latency (config
+        # 4 at one arrival rate) and batched solves/s (config 3)
+        del W, out, ctl, Wh, Oh
+        torch.cuda.empty_cache()
+        line["serving"] = measure_serving(torch, tg, dev, args.serve_rate, args.serve_requests)
+        line["batching"] = measure_batching(torch, tg, dev, 256, 100, 3)
     emit(line, args.out)
     return 0
 
@@ -334,26 +351,26 @@ def _gpu_setup():
     return torch, tg, dev
 
 
-def run_batch_workload(args):
+def measure_batching(torch, tg, dev, instances=256, K=100, warmup=3):
     """Config 3: `instances` overpressure spheres, N uniform in {32,48,64,96,128},
     radius U[0.05,0.2], pressure ratio U[10,100] (p_out 0.1), +-1% rho noise,
-    100 CFL steps each with its own dt, in one persistent graph-captured launch;
+    K CFL steps each with its own dt, in one persistent graph-captured launch;
     against the plain loop of one run_steps call per instance."""
     import numpy as np
-    torch, tg, dev = _gpu_setup()
     from tinyfluids_gb300.batching import Batch, InstanceSpec
     rng = np.random.default_rng(0)
-    K = args.steps if args.steps != 200 else 100
     specs = []
-    for i in range(args.instances):
+    for i in range(instances):
         n = int(rng.choice([32, 48, 64, 96, 128]))
         ratio = float(rng.uniform(10, 100))
         W, dx = tg.overpressure(n, seed=i, radius=float(rng.uniform(0.05, 0.2)),
                                p_in=0.1 * ratio, p_out=0.1, device=dev)
         specs.append(InstanceSpec(W, dx, GAMMA, num_steps=K))
     cells = sum(sp.state[0].numel() for sp in specs) * K
+    t_tune = time.perf_counter()
     b = Batch(specs, autotune=True, capture_graph=True)
-    for _ in range(max(3, args.warmup)):
+    t_tune = time.perf_counter() - t_tune
+    for _ in range(max(3, warmup)):
         b.run()
     torch.cuda.synchronize()
     st = torch.cuda.current_stream(dev)
@@ -383,55 +400,68 @@ def run_batch_workload(args):
         r = tg.run_steps(sp.state, sp.grid_spacing, GAMMA, K, tile="auto")
         float(r[0, 0, 0, 0])  # the solve's result reaches the host
     ms_sync = (time.perf_counter() - t0) * 1e3
-    line = {"metric": "batched solves/s (256 uneven instances, 100 CFL steps each)",
-            "value": args.instances / (ms_batch * 1e-3), "unit": "solves/s",
-            "higher_is_better": True, "n_gpus": 1, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{args.instances} overpressure instances, N in "
-                                   "{32,48,64,96,128}, 100 steps, persistent launch",
-                       "rows": b.rows},
-            "gcell_updates_per_s": cells / (ms_batch * 1e-3) / 1e9, "ms": ms_batch,
-            "plain_loop_async": {"solves_per_s": args.instances / (ms_plain * 1e-3),
-                                 "ms": ms_plain,
-                                 "gcell_updates_per_s": cells / (ms_plain * 1e-3) / 1e9},
-            "plain_loop_one_at_a_time": {"solves_per_s": args.instances / (ms_sync * 1e-3),
-                                         "ms": ms_sync,
-                                         "gcell_updates_per_s": cells / (ms_sync * 1e-3) / 1e9},
-            "speedup_vs_plain_loop_async": ms_plain / ms_batch,
-            "speedup_vs_plain_loop_one_at_a_time": ms_sync / ms_batch,
-            "results_equal_alone": bool(same)}
+    res = {"solves_per_s": instances / (ms_batch * 1e-3), "ms": ms_batch,
+           "gcell_updates_per_s": cells / (ms_batch * 1e-3) / 1e9,
+           "workload": f"{instances} overpressure instances, N in {{32,48,64,96,128}}, "
+                       f"{K} CFL steps each, one persistent graph-captured launch",
+           "rows": b.rows, "tuning_s": t_tune,
+           "plain_loop_async": {"solves_per_s": instances / (ms_plain * 1e-3), "ms": ms_plain,
+                                "gcell_updates_per_s": cells / (ms_plain * 1e-3) / 1e9},
+           "plain_loop_one_at_a_time": {"solves_per_s": instances / (ms_sync * 1e-3),
+                                        "ms": ms_sync,
+                                        "gcell_updates_per_s": cells / (ms_sync * 1e-3) / 1e9},
+           "speedup_vs_plain_loop_async": ms_plain / ms_batch,
+           "speedup_vs_plain_loop_one_at_a_time": ms_sync / ms_batch,
+           "results_equal_alone": bool(same)}
+    b.close()
+    return res
+
+
+def measure_serving(torch, tg, dev, rate, requests):
+    """Config 4 at one arrival rate: Poisson arrivals, N uniform in [32,256],
+    steps uniform in [50,500], seeded overpressure or shear states, 120 GB
+    budget; the continuous-batching server (SRPT ticks) against the plain
+    one-solve-at-a-time loop on the same requests."""
+    from tinyfluids_gb300 import serving
+
+    def fresh(reqs):
+        return [serving.Request(r.rid, r.n, r.steps, r.ic, r.seed, r.arrival) for r in reqs]
+
+    # warm-up: first use of the kernels, batch plans and allocator in this
+    # process, outside the measurement (both arms)
+    warm = serving.poisson_requests(12, 200.0, seed=12345)
+    serving.Server(hbm_budget=120e9, device=dev, policy="srpt").serve(fresh(warm))
+    serving.serve_one_at_a_time(fresh(warm), device=dev)
+    torch.cuda.synchronize()
+    reqs = serving.poisson_requests(requests, rate, seed=int(rate))
+    srv = serving.Server(hbm_budget=120e9, device=dev, policy="srpt")
+    st = serving.latency_stats(srv.serve(fresh(reqs)))
+    bt = serving.latency_stats(serving.serve_one_at_a_time(fresh(reqs), device=dev))
+    return {"rate_req_per_s": rate, "requests": requests,
+            "workload": f"{requests} Poisson requests at {rate:g} req/s, N U[32,256], steps "
+                        "U[50,500], overpressure or shear, 120 GB admission budget",
+            "served": st, "one_at_a_time": bt, "ticks": srv.ticks,
+            "solves_per_s_ratio": st["solves_per_s"] / bt["solves_per_s"],
+            "p50_ratio": bt["p50_s"] / st["p50_s"], "p99_ratio": bt["p99_s"] / st["p99_s"]}
+
+
+def run_batch_workload(args):
+    torch, tg, dev = _gpu_setup()
+    K = args.steps if args.steps != 200 else 100
+    r = measure_batching(torch, tg, dev, args.instances, K, args.warmup)
+    line = {"metric": f"batched solves/s ({args.instances} uneven instances, {K} CFL steps each)",
+            "value": r["solves_per_s"], "unit": "solves/s", "higher_is_better": True,
+            "n_gpus": 1, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": r["workload"], "rows": r["rows"]}, **r}
     emit(line, args.out)
     return 0
 
 
 def run_serve_workload(args):
-    """Config 4: Poisson arrivals over a rate sweep; N uniform in [32,256],
-    steps uniform in [50,500], seeded overpressure or shear states, 120 GB
-    budget; continuous batching against the plain one-solve-at-a-time loop."""
+    """Config 4 over a rate sweep."""
     torch, tg, dev = _gpu_setup()
-    from tinyfluids_gb300 import serving
     rates = [float(r) for r in args.rates.split(",")]
-    sweep = []
-    def fresh(reqs):
-        return [serving.Request(r.rid, r.n, r.steps, r.ic, r.seed, r.arrival) for r in reqs]
-
-    # warm-up: first use of the kernels, batch plans and allocator in this
-    # process, outside the measured sweep (all three arms)
-    warm = serving.poisson_requests(12, 200.0, seed=12345)
-    serving.Server(hbm_budget=120e9, device=dev, policy="srpt").serve(fresh(warm))
-    serving.Server(hbm_budget=120e9, device=dev, policy="all").serve(fresh(warm))
-    serving.serve_one_at_a_time(fresh(warm), device=dev)
-    torch.cuda.synchronize()
-    for rate in rates:
-        reqs = serving.poisson_requests(args.requests, rate, seed=int(rate))
-        srv = serving.Server(hbm_budget=120e9, device=dev, policy="srpt")
-        st = serving.latency_stats(srv.serve(fresh(reqs)))
-        srv_all = serving.Server(hbm_budget=120e9, device=dev, policy="all")
-        st_all = serving.latency_stats(srv_all.serve(fresh(reqs)))
-        bt = serving.latency_stats(serving.serve_one_at_a_time(fresh(reqs), device=dev))
-        sweep.append({"rate": rate, "served": st, "served_all_in_every_tick": st_all,
-                      "one_at_a_time": bt, "ticks": srv.ticks,
-                      "solves_per_s_ratio": st["solves_per_s"] / bt["solves_per_s"],
-                      "p50_ratio": bt["p50_s"] / st["p50_s"]})
+    sweep = [measure_serving(torch, tg, dev, rate, args.requests) for rate in rates]
     top = sweep[-1]
     line = {"metric": "served solves/s, p50/p99 latency (continuous batching, SRPT ticks)",
             "value": top["served"]["solves_per_s"], "unit": "solves/s", "higher_is_better": True,
