@@ -46,6 +46,12 @@ namespace tf {
 #ifndef TF_PF_DEPTH
 #define TF_PF_DEPTH 2
 #endif
+// TF_ALT_CARRY 1 (with TF_PF_DEPTH 1): two planes per loop trip with the
+// carried plane quantities alternating between two register sets instead of
+// being copied after every plane.
+#ifndef TF_ALT_CARRY
+#define TF_ALT_CARRY 0
+#endif
 // Ring warp: the tile's two ring rows (the rows above and below the stored
 // rows) are held by the last warp, which sweeps them along x and contributes
 // the y faces at the tile edges but skips the y update, the z sweep and the
@@ -399,7 +405,17 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
     __syncthreads();
     return false;
   };
-#if TF_PF_DEPTH == 1
+#if TF_PF_DEPTH == 1 && TF_ALT_CARRY
+  // one plane in flight, carry roles alternating: after the trip's second
+  // plane the carry is back in c0 / f0
+  for (int x = t.x0; x < t.x_end; x += 2) {
+    plane_update<P, NWP, DIAG, RING>(x, pb, c0, f0, c1, f1, K, sm, o,
+                               [&]() { if (x + 2 <= t.x_end) load(x + 2, pb); }, sync_only);
+    if (x + 1 < t.x_end)
+      plane_update<P, NWP, DIAG, RING>(x + 1, pb, c1, f1, c0, f0, K, sm, o,
+                                 [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); }, sync_only);
+  }
+#elif TF_PF_DEPTH == 1
   // one plane in flight: pb holds plane x+1 on entry and receives plane x+2
   for (int x = t.x0; x < t.x_end; ++x) {
     plane_update<P, NWP, DIAG, RING>(x, pb, c0, f0, c1, f1, K, sm, o,
