@@ -323,7 +323,7 @@ int tf_batch_prepare(const tf_instance* inst, int count, const tf_batch_config* 
   plan.count = count;
   if (cfg) {
     if (!valid_tile_rows(cfg->rows))
-      return set_error(TF_ERR_ARG, "batch rows must be 8, 16, 18 or 32 (got %d)", cfg->rows);
+      return set_error(TF_ERR_ARG, "batch rows must be 8, 16 or 32 (got %d)", cfg->rows);
     plan.rows = cfg->rows;
     plan.exact = cfg->exact ? 1 : 0;
     plan.persistent = cfg->persistent ? 1 : 0;

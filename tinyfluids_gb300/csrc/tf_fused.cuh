@@ -36,30 +36,6 @@
 
 namespace tf {
 
-// Build switches of the fused tile (defaults: the measured-best form).
-// TF_ADDR 1: 32-bit element offsets for loads and stores (states of at most
-// 2^31 floats) instead of 64-bit address arithmetic per access.
-#ifndef TF_ADDR
-#define TF_ADDR 0
-#endif
-// Planes in flight per thread (register prefetch): 2 or 1.
-#ifndef TF_PF_DEPTH
-#define TF_PF_DEPTH 2
-#endif
-// TF_ALT_CARRY 1 (with TF_PF_DEPTH 1): two planes per loop trip with the
-// carried plane quantities alternating between two register sets instead of
-// being copied after every plane.
-#ifndef TF_ALT_CARRY
-#define TF_ALT_CARRY 0
-#endif
-// Ring warp: the tile's two ring rows (the rows above and below the stored
-// rows) are held by the last warp, which sweeps them along x and contributes
-// the y faces at the tile edges but skips the y update, the z sweep and the
-// stores; the other warps hold stored rows only.
-#ifndef TF_RINGWARP
-#define TF_RINGWARP 0
-#endif
-
 constexpr int kTileLanes = 32;          // lanes per tile row (z)
 constexpr int kTileZ = kTileLanes - 2;  // stored z cells per tile row
 
@@ -151,12 +127,6 @@ static __device__ long long g_chk_ncells;
 
 __device__ __forceinline__ void store5(const TileOut& o, int x, size_t dcol, const V2 wo[5],
                                        bool hi) {
-#if TF_ADDR == 1 && !TF_CHECKED
-  const unsigned oc = (unsigned)x * (unsigned)o.plane + (unsigned)dcol;
-#pragma unroll
-  for (int i = 0; i < 5; ++i) o.dst[oc + (unsigned)i * (unsigned)o.vstride] = hi ? wo[i].y : wo[i].x;
-  return;
-#endif
   float* q = o.dst + (size_t)x * o.plane + dcol;
 #if TF_CHECKED
   const size_t cell = (size_t)x * o.plane + dcol;
@@ -177,8 +147,7 @@ __device__ __forceinline__ void store5(const TileOut& o, int x, size_t dcol, con
 // `after_sync()` runs after the plane's first CTA barrier, when every thread
 // has read plane x+1 (the TMA loader refills its stage there) and returns
 // true if the CTA must stop (a bounded wait gave up).
-template <class P, int NWP, bool DIAG = false, bool RING = false, class Consumed,
-          class AfterSync>
+template <class P, int NWP, bool DIAG = false, class Consumed, class AfterSync>
 __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, const V2 fm[5],
                                              Cell2& nxt, V2 fp[5], const StepConsts<float>& K,
                                              FusedSmem<NWP>& sm, TileOut& o, Consumed consumed,
@@ -208,12 +177,10 @@ __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, 
   Cell2 L;
   {
     float4 a, b, d;
-    if (RING || w >= 1) {
-      // with a ring warp, warp 0's cell above is the ring warp's lower cell
-      const int wa = RING ? (w + NWP - 1) % NWP : w - 1;
-      a = sm.cy[0][wa][lane];
-      b = sm.cy[1][wa][lane];
-      d = sm.cy[2][wa][lane];
+    if (w >= 1) {
+      a = sm.cy[0][w - 1][lane];
+      b = sm.cy[1][w - 1][lane];
+      d = sm.cy[2][w - 1][lane];
     } else {
       a = make_float4(cy.U[0].x, cy.U[1].x, cy.U[2].x, cy.U[3].x);
       b = make_float4(cy.U[4].x, cy.F[0].x, cy.F[1].x, cy.F[2].x);
@@ -231,7 +198,6 @@ __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, 
   sm.fy4[w][lane] = make_float4(fy[0].x, fy[1].x, fy[2].x, fy[3].x);
   sm.fy1[w][lane] = fy[4].x;
   __syncthreads();
-  if (RING && w == NWP - 1) return stop;  // the ring warp's rows are not updated
   // face below the pair = the next warp's face above its pair; the last
   // warp's lower row is the ring and takes its own value (unused)
   V2 fyh[5];
@@ -287,7 +253,7 @@ struct TileCols {
   size_t col_a, col_b;  // source columns (wrapped / clamped)
 };
 
-template <int NWP, bool RING = false>
+template <int NWP>
 __device__ __forceinline__ TileCols tile_cols(const FusedGeom& G, int tz, int ty, int tx,
                                               const float* src, float* dst, TileOut& o) {
   const int lane = threadIdx.x & 31;
@@ -298,15 +264,8 @@ __device__ __forceinline__ TileCols tile_cols(const FusedGeom& G, int tz, int ty
   t.x0 = tx * G.lx;
   t.x_end = min(t.x0 + G.lx, G.nx);
   t.z = z0 - 1 + lane;
-  if (RING) {
-    // warps 0..NWP-2: rows y0 + 2w, y0 + 2w + 1 (stored); the ring warp: the
-    // row below the tile (upper cell) and the row above it (lower cell)
-    t.ya = w < NWP - 1 ? y0 + 2 * w : y0 + tile_rows_out(NWP);
-    t.yb = w < NWP - 1 ? t.ya + 1 : y0 - 1;
-  } else {
-    t.ya = y0 - 1 + 2 * w;
-    t.yb = t.ya + 1;
-  }
+  t.ya = y0 - 1 + 2 * w;
+  t.yb = t.ya + 1;
   const int zs = src_index(t.z, G.nz, open);
   t.col_a = (size_t)src_index(t.ya, G.ny, open) * G.nz + zs;
   t.col_b = (size_t)src_index(t.yb, G.ny, open) * G.nz + zs;
@@ -314,7 +273,7 @@ __device__ __forceinline__ TileCols tile_cols(const FusedGeom& G, int tz, int ty
   o.plane = (size_t)G.ny * G.nz;
   o.vstride = o.plane * G.nx;
   const bool store_lane = lane >= 1 && lane <= kTileLanes - 2 && t.z < G.nz;
-  o.store_a = store_lane && (RING ? w < NWP - 1 : w >= 1) && t.ya < G.ny;
+  o.store_a = store_lane && w >= 1 && t.ya < G.ny;
   o.store_b = store_lane && w <= NWP - 2 && t.yb < G.ny;
   o.dcol_a = o.store_a ? (size_t)t.ya * G.nz + t.z : 0;
   o.dcol_b = o.store_b ? (size_t)t.yb * G.nz + t.z : 0;
@@ -336,9 +295,8 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
                                             const StepConsts<float>& K, FusedSmem<NWP>& sm,
                                             DiagArgs d = DiagArgs{nullptr, -1},
                                             CSum* acc = nullptr) {
-  constexpr bool RING = TF_RINGWARP != 0;
   TileOut o;
-  const TileCols t = tile_cols<NWP, RING>(G, tz, ty, tx, src, dst, o);
+  const TileCols t = tile_cols<NWP>(G, tz, ty, tx, src, dst, o);
   if constexpr (DIAG) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) o.acc[i] = CSum{0.f, 0.f};
@@ -362,18 +320,6 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
 #else
   auto ld = [&](const float* p) { return COHERENT ? __ldcg(p) : __ldg(p); };
 #endif
-#if TF_ADDR == 1 && !TF_CHECKED
-  const unsigned ca32 = (unsigned)t.col_a, cb32 = (unsigned)t.col_b;
-  auto load = [&](int x, V2 v[5]) {
-    const unsigned xo = (unsigned)src_index(x, G.nx, open) * (unsigned)o.plane;
-    const unsigned oa = xo + ca32, ob = xo + cb32;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      v[i].x = ld(src + (oa + (unsigned)i * (unsigned)o.vstride));
-      v[i].y = ld(src + (ob + (unsigned)i * (unsigned)o.vstride));
-    }
-  };
-#else
   auto load = [&](int x, V2 v[5]) {
     const float* p = src + (size_t)src_index(x, G.nx, open) * o.plane;
 #pragma unroll
@@ -383,10 +329,14 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
       v[i].y = ld(q + t.col_b);
     }
   };
-#endif
-  // carried plane quantities: c0 = plane x, c1 receives plane x+1 (copying
-  // it back measured fewer live registers than alternating the two roles)
-  Cell2 c0, c1;
+  // Loop form: the fast arithmetic's plain tile keeps one plane in flight and
+  // alternates the carried plane quantities between two register sets (two
+  // planes per trip, no copy); measured 3.6% faster at 512^3 than the form
+  // below, which the other instantiations keep because the alternating form
+  // spills registers there: two planes in flight and the carry copied back
+  // after every plane.
+  constexpr bool kAlt = !DIAG && !P::kExact;
+  Cell2 c0, c1;  // c0 = plane x, c1 receives plane x+1
   V2 f0[5], f1[5];
   V2 pa[5], pb[5];
   {
@@ -398,50 +348,43 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
     P::template derive<1>(s, c1, K);
     P::to_state(pa, s, K);
     P::template derive<1>(s, c0, K);
-    if (TF_PF_DEPTH == 2 && t.x0 + 2 <= t.x_end) load(t.x0 + 2, pa);
+    if (!kAlt && t.x0 + 2 <= t.x_end) load(t.x0 + 2, pa);
     P::hll(c1, c0, f0);  // flux at face x0 - 1/2; c0 = plane x0
   }
   auto sync_only = []() {
     __syncthreads();
     return false;
   };
-#if TF_PF_DEPTH == 1 && TF_ALT_CARRY
-  // one plane in flight, carry roles alternating: after the trip's second
-  // plane the carry is back in c0 / f0
-  for (int x = t.x0; x < t.x_end; x += 2) {
-    plane_update<P, NWP, DIAG, RING>(x, pb, c0, f0, c1, f1, K, sm, o,
-                               [&]() { if (x + 2 <= t.x_end) load(x + 2, pb); }, sync_only);
-    if (x + 1 < t.x_end)
-      plane_update<P, NWP, DIAG, RING>(x + 1, pb, c1, f1, c0, f0, K, sm, o,
+  if constexpr (kAlt) {
+    // pb holds plane x+1 on entry and receives plane x+2; after the trip's
+    // second plane the carry is back in c0 / f0
+    for (int x = t.x0; x < t.x_end; x += 2) {
+      plane_update<P, NWP, DIAG>(x, pb, c0, f0, c1, f1, K, sm, o,
+                                 [&]() { if (x + 2 <= t.x_end) load(x + 2, pb); }, sync_only);
+      if (x + 1 < t.x_end)
+        plane_update<P, NWP, DIAG>(x + 1, pb, c1, f1, c0, f0, K, sm, o,
+                                   [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); },
+                                   sync_only);
+    }
+  } else {
+    // Two planes per trip so the prefetch buffers alternate without moves;
+    // `pf` holds plane x+1 on entry and receives plane x+3.
+    for (int x = t.x0; x < t.x_end; x += 2) {
+      plane_update<P, NWP, DIAG>(x, pb, c0, f0, c1, f1, K, sm, o,
                                  [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); }, sync_only);
-  }
-#elif TF_PF_DEPTH == 1
-  // one plane in flight: pb holds plane x+1 on entry and receives plane x+2
-  for (int x = t.x0; x < t.x_end; ++x) {
-    plane_update<P, NWP, DIAG, RING>(x, pb, c0, f0, c1, f1, K, sm, o,
-                               [&]() { if (x + 2 <= t.x_end) load(x + 2, pb); }, sync_only);
-    c0 = c1;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) f0[i] = f1[i];
-  }
-#else
-  // Two planes per trip so the prefetch buffers alternate without moves;
-  // `pf` holds plane x+1 on entry and receives plane x+3.
-  for (int x = t.x0; x < t.x_end; x += 2) {
-    plane_update<P, NWP, DIAG, RING>(x, pb, c0, f0, c1, f1, K, sm, o,
-                               [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); }, sync_only);
-    c0 = c1;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) f0[i] = f1[i];
-    if (x + 1 < t.x_end) {
-      plane_update<P, NWP, DIAG, RING>(x + 1, pa, c0, f0, c1, f1, K, sm, o,
-                                 [&]() { if (x + 4 <= t.x_end) load(x + 4, pa); }, sync_only);
       c0 = c1;
 #pragma unroll
       for (int i = 0; i < 5; ++i) f0[i] = f1[i];
+      if (x + 1 < t.x_end) {
+        plane_update<P, NWP, DIAG>(x + 1, pa, c0, f0, c1, f1, K, sm, o,
+                                   [&]() { if (x + 4 <= t.x_end) load(x + 4, pa); },
+                                   sync_only);
+        c0 = c1;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) f0[i] = f1[i];
+      }
     }
   }
-#endif
   if constexpr (DIAG) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) acc[i] = o.acc[i];

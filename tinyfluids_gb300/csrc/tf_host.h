@@ -38,32 +38,19 @@ inline RowLaunch row_launch(int nx, int ny, int nz) {
 
 // Tile heights (grid rows incl. the one-cell ring) the fused kernel is
 // instantiated for; the kernel uses rows/2 warps.
-inline bool valid_tile_rows(int rows) {
-  return rows == 8 || rows == 16 || rows == 18 || rows == 32;
-}
+inline bool valid_tile_rows(int rows) { return rows == 8 || rows == 16 || rows == 32; }
 
 // CTAs per SM the fused kernels are register-bounded for: TF_WARPS_PER_SM
-// (18 by default) warps per SM, rounded down to whole CTAs: two CTAs of 8 or
-// 9 warps, four of 4, one of 16.
+// (16 by default) warps per SM for every tile height.
 #ifndef TF_WARPS_PER_SM
-#define TF_WARPS_PER_SM 18
+#define TF_WARPS_PER_SM 16
 #endif
 __host__ __device__ constexpr int min_ctas_per_sm(int nwp) {
   return nwp >= TF_WARPS_PER_SM ? 1 : TF_WARPS_PER_SM / nwp;
 }
 
-// Register cap of a fused kernel of nwp warps: the 64K registers of an SM
-// shared by min_ctas_per_sm(nwp) CTAs, in units of 8 per thread, at most 128.
-// Given explicitly: the cap the compiler derives from a minimum CTA count
-// rounds 9-warp CTAs down to 96 registers although 112 fit twice.
-__host__ __device__ constexpr int fused_maxnreg(int nwp) {
-  return (65536 / (min_ctas_per_sm(nwp) * nwp * 32)) / 8 * 8 > 128
-             ? 128
-             : (65536 / (min_ctas_per_sm(nwp) * nwp * 32)) / 8 * 8;
-}
-
 // Launch bounds of the fused-step kernels (single step, TMA form, batch).
-#define TF_FUSED_BOUNDS(NWP) __launch_bounds__((NWP) * 32) __maxnreg__(fused_maxnreg(NWP))
+#define TF_FUSED_BOUNDS(NWP) __launch_bounds__((NWP) * 32, min_ctas_per_sm(NWP))
 
 #define TF_DISPATCH_ROWS(rows, NWP, ...)          \
   switch (rows) {                                 \
@@ -73,10 +60,6 @@ __host__ __device__ constexpr int fused_maxnreg(int nwp) {
     } break;                                      \
     case 16: {                                    \
       constexpr int NWP = 8;                      \
-      __VA_ARGS__;                                \
-    } break;                                      \
-    case 18: {                                    \
-      constexpr int NWP = 9;                      \
       __VA_ARGS__;                                \
     } break;                                      \
     default: {                                    \

@@ -10,7 +10,6 @@
 
 #include "tf_common.cuh"
 #include "tf_fused.cuh"
-#include "tf_fused_xp.cuh"
 #include "tf_host.h"
 #include "tf_math.cuh"
 
@@ -357,37 +356,6 @@ __global__ void TF_FUSED_BOUNDS(NWP) fused_step_kernel(FusedArgs a) {
   }
 }
 
-// The fused step with plane pairs (fused_tile_xp): NW warps, one tile row
-// each, shared memory sized at launch (above the 48 KB static limit for 16
-// warps).
-#ifndef TF_XP
-#define TF_XP 0
-#endif
-template <class P, int NW>
-__global__ void __maxnreg__(128) fused_step_xp_kernel(FusedArgs a) {
-  extern __shared__ __align__(16) unsigned char xp_smem[];
-  FusedSmemXP<NW>& sm = *reinterpret_cast<FusedSmemXP<NW>*>(xp_smem);
-  float dt;
-  if (!launch_dt(a, &dt)) return;
-  const StepConsts<float> K = launch_consts(a, dt);
-  float m = fused_tile_xp<P, NW>(a.src, a.dst, a.geo, blockIdx.x, blockIdx.y, blockIdx.z, K, sm);
-  if (a.ctl) {
-    float bm = block_max(m, sm.red);
-    if (threadIdx.x == 0)
-      ctl_finish_cta(a.ctl, bm, gridDim.x * gridDim.y * gridDim.z, dt, a.loop != 0);
-  }
-}
-
-template <class P, int NW>
-static int launch_xp(const FusedArgs& a, dim3 grid, cudaStream_t s) {
-  auto k = fused_step_xp_kernel<P, NW>;
-  const int smem = (int)sizeof(FusedSmemXP<NW>);
-  TF_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
-                    "cudaFuncSetAttribute"));
-  k<<<grid, NW * 32, smem, s>>>(a);
-  return launch_check("fused_step_xp_kernel");
-}
-
 // The fused step with TMA-staged planes (fused_tile_tma); the tensor map
 // describes a.src.
 template <class P, int NWP>
@@ -517,7 +485,7 @@ static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx, int* loa
   *loader = 0;
   if (tile) {
     if (!valid_tile_rows(tile->rows))
-      return set_error(TF_ERR_ARG, "tile rows must be 8, 16, 18 or 32 (got %d)", tile->rows);
+      return set_error(TF_ERR_ARG, "tile rows must be 8, 16 or 32 (got %d)", tile->rows);
     *rows = tile->rows;
     *lx = tile->lx;
     if (*lx < 0) return set_error(TF_ERR_ARG, "tile lx must be >= 0");
@@ -554,16 +522,6 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
       TF_DISPATCH_ROWS(rows, NWP, TF_TRY((launch_tma<NWP>(a, grid, tm, exact, s))));
       return launch_check("fused_step_tma_kernel");
     }
-  }
-  if (TF_XP && !a.totals && (rows == 16 || rows == 8)) {
-    if (a.conserved_io) {
-      if (exact || rows != 16)
-        return set_error(TF_ERR_UNSUPPORTED,
-                         "conserved input/output: fast arithmetic and 16-row tiles only");
-      return launch_xp<FastPairConserved, 16>(a, grid, s);
-    }
-    if (rows == 16) return exact ? launch_xp<ExactPair, 16>(a, grid, s) : launch_xp<FastPair, 16>(a, grid, s);
-    return exact ? launch_xp<ExactPair, 8>(a, grid, s) : launch_xp<FastPair, 8>(a, grid, s);
   }
   if (a.totals) {
     TF_DISPATCH_ROWS(rows, NWP, {
