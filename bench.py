@@ -258,6 +258,20 @@ def run_gpu(args):
     if summ["status"] != 0 or summ["iter"] != K:
         raise RuntimeError(f"run failed: {summ}")
     cells = n ** 3
+    # the fused kernel's own launch duration: a second run of K - K/2 fewer
+    # steps, timed the same way; the per-run work (control block, CFL
+    # reduction of the initial state, final buffer choice) cancels in the
+    # difference
+    Kh = K // 2
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    e2.record(stream)
+    tg.run_steps(W, dx, GAMMA, Kh, tile=tile)
+    e3.record(stream)
+    barrier()
+    ms_half = e2.elapsed_time(e3)
+    kernel_ms = (ms - ms_half) / (K - Kh) if K > Kh else ms / max(K, 1)
     value, ms = replicas.job_throughput(cells, K, ms, world, dev)
 
     # ---- end to end: public API with pinned host buffers ----
@@ -290,7 +304,7 @@ def run_gpu(args):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    per_launch_ms = ms / K
+    per_launch_ms = kernel_ms
     achieved = BYTES_PER_CELL * cells / (per_launch_ms * 1e-3) / 1e9
     traffic = None
     prof = os.path.join(ROOT, "profiles", "fused_step_traffic.json")
@@ -317,8 +331,10 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_src,
-                     "kernel": "fused_step_kernel (40 B/cell algorithmic; duration = run "
-                               "time / steps, incl. the one-off dt init)"},
+                     "kernel": "fused_step_kernel (40 B/cell algorithmic)",
+                     "launch_ms": per_launch_ms,
+                     "launch_ms_definition": f"(time of {K} steps - time of {Kh} steps) / "
+                                             f"{K - Kh}, CUDA events on the launching stream"},
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": state_bytes / K, "d2h_bytes_per_step": state_bytes / K,
                 "definition": f"pinned host state -> device, {K} steps, state -> pinned host; "

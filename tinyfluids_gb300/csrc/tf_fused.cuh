@@ -46,6 +46,16 @@ struct FusedGeom {
   int open_bc;                    // TF_FLAG_OPEN_BOUNDARIES set
 };
 
+// Per-variable base pointers of a launch's source and destination states
+// (variable i of a [5][nx][ny][nz] state starts i * nx*ny*nz floats in), for
+// kernels that receive them as launch parameters: an access is then a 32-bit
+// element offset within one variable added to a parameter-space base, with
+// no 64-bit address arithmetic per access.  Needs nx*ny*nz < 2^31.
+struct VarPtrs {
+  const float* s[5];
+  float* d[5];
+};
+
 // stored rows per tile for NWP warps (two rows per warp, minus the ring)
 __host__ __device__ constexpr int tile_rows_out(int nwp) { return 2 * nwp - 2; }
 
@@ -73,6 +83,7 @@ __device__ __forceinline__ void shfl_up_cell2(const Cell2& in, Cell2& out) {
 
 // Per-thread context of one tile: store targets and the running CFL speed.
 struct TileOut {
+  const VarPtrs* vp;  // per-variable bases (launch parameters), or null
   float* dst;
   size_t plane, vstride, dcol_a, dcol_b;
   bool store_a, store_b;
@@ -125,8 +136,15 @@ static __device__ int* g_chk_writes;
 static __device__ long long g_chk_ncells;
 #endif
 
+template <bool VP = false>
 __device__ __forceinline__ void store5(const TileOut& o, int x, size_t dcol, const V2 wo[5],
                                        bool hi) {
+  if constexpr (VP && !TF_CHECKED) {
+    const unsigned oc = (unsigned)x * (unsigned)o.plane + (unsigned)dcol;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) o.vp->d[i][oc] = hi ? wo[i].y : wo[i].x;
+    return;
+  }
   float* q = o.dst + (size_t)x * o.plane + dcol;
 #if TF_CHECKED
   const size_t cell = (size_t)x * o.plane + dcol;
@@ -147,7 +165,8 @@ __device__ __forceinline__ void store5(const TileOut& o, int x, size_t dcol, con
 // `after_sync()` runs after the plane's first CTA barrier, when every thread
 // has read plane x+1 (the TMA loader refills its stage there) and returns
 // true if the CTA must stop (a bounded wait gave up).
-template <class P, int NWP, bool DIAG = false, class Consumed, class AfterSync>
+template <class P, int NWP, bool DIAG = false, bool VP = false, class Consumed,
+          class AfterSync>
 __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, const V2 fm[5],
                                              Cell2& nxt, V2 fp[5], const StepConsts<float>& K,
                                              FusedSmem<NWP>& sm, TileOut& o, Consumed consumed,
@@ -235,12 +254,12 @@ __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, 
   P::update(cz, fzl, fzh, s3, K);
   const V2 sp = P::finish(s3, wo, K);
   if (o.store_a) {
-    store5(o, x, o.dcol_a, wo, false);
+    store5<VP>(o, x, o.dcol_a, wo, false);
     o.wmax = speed_max(o.wmax, sp.x);
     if constexpr (DIAG) diag_cell(o, x, o.sy_a, wo, false, K);
   }
   if (o.store_b) {
-    store5(o, x, o.dcol_b, wo, true);
+    store5<VP>(o, x, o.dcol_b, wo, true);
     o.wmax = speed_max(o.wmax, sp.y);
     if constexpr (DIAG) diag_cell(o, x, o.sy_b, wo, true, K);
   }
@@ -289,14 +308,16 @@ __device__ __forceinline__ TileCols tile_cols(const FusedGeom& G, int tz, int ty
 // use the read-only path.
 // DIAG: also accumulate the stored cells' conserved totals into acc[5] and
 // write the slice of `d` (the diagnostics instantiation of the single step).
-template <class P, int NWP, bool COHERENT = false, bool DIAG = false>
+// VP: `vp` holds the per-variable bases of src and dst as launch parameters.
+template <class P, int NWP, bool COHERENT = false, bool DIAG = false, bool VP = false>
 __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float* __restrict__ dst,
                                             const FusedGeom& G, int tz, int ty, int tx,
                                             const StepConsts<float>& K, FusedSmem<NWP>& sm,
                                             DiagArgs d = DiagArgs{nullptr, -1},
-                                            CSum* acc = nullptr) {
+                                            CSum* acc = nullptr, const VarPtrs* vp = nullptr) {
   TileOut o;
   const TileCols t = tile_cols<NWP>(G, tz, ty, tx, src, dst, o);
+  o.vp = vp;
   if constexpr (DIAG) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) o.acc[i] = CSum{0.f, 0.f};
@@ -320,13 +341,24 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
 #else
   auto ld = [&](const float* p) { return COHERENT ? __ldcg(p) : __ldg(p); };
 #endif
+  const unsigned ca32 = (unsigned)t.col_a, cb32 = (unsigned)t.col_b;
   auto load = [&](int x, V2 v[5]) {
-    const float* p = src + (size_t)src_index(x, G.nx, open) * o.plane;
+    if constexpr (VP && !TF_CHECKED) {
+      const unsigned xo = (unsigned)src_index(x, G.nx, open) * (unsigned)o.plane;
+      const unsigned oa = xo + ca32, ob = xo + cb32;
 #pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      const float* q = p + i * o.vstride;
-      v[i].x = ld(q + t.col_a);
-      v[i].y = ld(q + t.col_b);
+      for (int i = 0; i < 5; ++i) {
+        v[i].x = ld(vp->s[i] + oa);
+        v[i].y = ld(vp->s[i] + ob);
+      }
+    } else {
+      const float* p = src + (size_t)src_index(x, G.nx, open) * o.plane;
+#pragma unroll
+      for (int i = 0; i < 5; ++i) {
+        const float* q = p + i * o.vstride;
+        v[i].x = ld(q + t.col_a);
+        v[i].y = ld(q + t.col_b);
+      }
     }
   };
   // Loop form: the fast arithmetic's plain tile keeps one plane in flight and
@@ -359,10 +391,10 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
     // pb holds plane x+1 on entry and receives plane x+2; after the trip's
     // second plane the carry is back in c0 / f0
     for (int x = t.x0; x < t.x_end; x += 2) {
-      plane_update<P, NWP, DIAG>(x, pb, c0, f0, c1, f1, K, sm, o,
-                                 [&]() { if (x + 2 <= t.x_end) load(x + 2, pb); }, sync_only);
+      plane_update<P, NWP, DIAG, VP>(x, pb, c0, f0, c1, f1, K, sm, o,
+                                     [&]() { if (x + 2 <= t.x_end) load(x + 2, pb); }, sync_only);
       if (x + 1 < t.x_end)
-        plane_update<P, NWP, DIAG>(x + 1, pb, c1, f1, c0, f0, K, sm, o,
+        plane_update<P, NWP, DIAG, VP>(x + 1, pb, c1, f1, c0, f0, K, sm, o,
                                    [&]() { if (x + 3 <= t.x_end) load(x + 3, pb); },
                                    sync_only);
     }

@@ -303,6 +303,7 @@ struct FusedArgs {
   // same for every thread of a CTA.
   const float* src;
   float* dst;
+  VarPtrs vp;  // per-variable bases of src and dst (set by launch_fused)
   FusedGeom geo;
   float gamma, inv_dx, gm1, igm1;
   float dt_host;
@@ -338,16 +339,18 @@ __device__ __forceinline__ StepConsts<float> launch_consts(const FusedArgs& a, f
   return K;
 }
 
-template <class P, int NWP, bool DIAG = false>
-__global__ void TF_FUSED_BOUNDS(NWP) fused_step_kernel(FusedArgs a) {
+// VP: per-variable bases from the launch parameters and 32-bit element
+// offsets (grids of fewer than 2^31 cells; the fast arithmetic's plain step).
+template <class P, int NWP, bool DIAG = false, bool VP = false>
+__global__ void TF_FUSED_BOUNDS(NWP) fused_step_kernel(const __grid_constant__ FusedArgs a) {
   __shared__ FusedSmem<NWP> sm;
   __shared__ double dred[DIAG ? NWP * 5 : 1];
   float dt;
   if (!launch_dt(a, &dt)) return;
   const StepConsts<float> K = launch_consts(a, dt);
   CSum acc[5];
-  float m = fused_tile<P, NWP, false, DIAG>(a.src, a.dst, a.geo, blockIdx.x, blockIdx.y,
-                                            blockIdx.z, K, sm, a.diag, acc);
+  float m = fused_tile<P, NWP, false, DIAG, VP && !DIAG && !P::kExact>(a.src, a.dst, a.geo, blockIdx.x, blockIdx.y,
+                                                blockIdx.z, K, sm, a.diag, acc, &a.vp);
   if constexpr (DIAG) block_add_totals(acc, dred, a.totals);
   if (a.ctl) {
     float bm = block_max(m, sm.red);
@@ -512,9 +515,16 @@ static int launch_tma(const FusedArgs& a, dim3 grid, const CUtensorMap& tm, bool
 // planes (falls back to loads when not usable).  Auto takes the per-thread
 // loads: on GB300 at 256^3-512^3 they measured faster (80 vs 64 Gcell/s at
 // 512^3 with 16-row tiles).
-static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s, int loader = 1) {
-  if (a.geo.tiles_y > 65535 || a.geo.tiles_x > 65535)
+static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_t s,
+                        int loader = 1) {
+  if (a_in.geo.tiles_y > 65535 || a_in.geo.tiles_x > 65535)
     return set_error(TF_ERR_ARG, "grid too large for the tile grid");
+  FusedArgs a = a_in;
+  const size_t vs = (size_t)a.geo.nx * a.geo.ny * a.geo.nz;
+  for (int i = 0; i < 5; ++i) {
+    a.vp.s[i] = a.src + i * vs;
+    a.vp.d[i] = a.dst ? a.dst + i * vs : nullptr;
+  }
   dim3 grid(a.geo.tiles_z, a.geo.tiles_y, a.geo.tiles_x);
   if (loader == 2 && tma_usable(a, rows)) {
     CUtensorMap tm;
@@ -534,11 +544,20 @@ static int launch_fused(const FusedArgs& a, int rows, bool exact, cudaStream_t s
     if (exact || rows != 16)
       return set_error(TF_ERR_UNSUPPORTED,
                        "conserved input/output: fast arithmetic and 16-row tiles only");
-    fused_step_kernel<FastPairConserved, 8><<<grid, 8 * 32, 0, s>>>(a);
+    if (vs < (1ull << 31))
+      fused_step_kernel<FastPairConserved, 8, false, true><<<grid, 8 * 32, 0, s>>>(a);
+    else
+      fused_step_kernel<FastPairConserved, 8><<<grid, 8 * 32, 0, s>>>(a);
     return launch_check("fused_step_kernel (conserved)");
   }
+#ifndef TF_NO_VP
+  const bool vp32 = vs < (1ull << 31);
+#else
+  const bool vp32 = false;
+#endif
   TF_DISPATCH_ROWS(rows, NWP, {
     if (exact) fused_step_kernel<ExactPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
+    else if (vp32) fused_step_kernel<FastPair, NWP, false, true><<<grid, NWP * 32, 0, s>>>(a);
     else fused_step_kernel<FastPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
   });
   return launch_check("fused_step_kernel");
