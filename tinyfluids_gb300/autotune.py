@@ -14,7 +14,10 @@ arithmetic) in memory and in a JSON file (``$TINYFLUIDS_GB300_TUNE_CACHE`` or
 Batches (``tune_batch``) are tuned on the batch itself: every (rows, lx
 policy) candidate runs a few steps of the actual batch and the fastest wins,
 because inside a full batch the best tile differs from the best tile for a
-grid running alone.
+grid running alone; then the chunk length is refined per size class (the
+instances of one grid size) on the batch.  The tile height stays one per
+launch: with 14 stored rows per 16-row tile, 16 rows is the best or an equal
+height for every size class of the batching workload (32-128 cells per axis).
 """
 from __future__ import annotations
 
@@ -139,42 +142,73 @@ def size_class(n: int) -> int:
     return SIZE_CLASSES[-1]
 
 
-def tune_batch(specs, exact=False, device=None, steps=2, candidates_rows=ROWS,
-               lx_policies=(0, 64, 32, 16, 8)):
-    """Tile choice for a batch: one `rows` for the launch and an `lx` per
-    instance.  Inside a batch the GPU is full, so single-grid timings are a
-    poor proxy; the candidates are timed on the batch itself (a short run of
-    `steps` steps on copies of its states).  lx policy 0 means the whole x
-    extent per CTA, otherwise min(nx, policy).  Cached per list of shapes."""
+def _time_batch(specs, rows, lxs, exact, dev, steps):
+    """Milliseconds of a short run (`steps` steps) of the batch on copies of
+    its states with per-instance chunk lengths `lxs`."""
     from dataclasses import replace
     from .batching import Batch
+    trial = [replace(sp, num_steps=steps, t_final=float("inf"), fixed_dt=None, lx=lx, out=None,
+                     consume_input=False)
+             for sp, lx in zip(specs, lxs)]
+    b = Batch(trial, rows=rows, exact=exact, autotune=False)
+    b.run()
+    st = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    b.run()
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    b.close()
+    return ms
+
+
+def tune_batch(specs, exact=False, device=None, steps=2, candidates_rows=ROWS,
+               lx_policies=(0, 64, 32, 16, 8), per_class=True):
+    """Tile choice for a batch: one `rows` for the launch and an `lx` per
+    instance.  Inside a batch the GPU is full, so single-grid timings are a
+    poor proxy; the candidates are timed on the batch itself (short runs of
+    `steps` steps on copies of its states).  First every (rows, lx policy)
+    pair is timed with the policy applied to all instances (policy 0: the
+    whole x extent per CTA, otherwise min(nx, policy)); then, per size class
+    (instances of the same grid size), each lx policy is tried for that
+    class alone with the other classes fixed, and kept if the batch gets
+    faster.  Returns (rows, [lx per instance]); cached per list of shapes."""
     shapes = tuple(tuple(sp.state.shape[1:]) for sp in specs)
     dev = torch.device(device if device is not None else specs[0].state.device)
-    key = ("batch", torch.cuda.get_device_name(dev), shapes, bool(exact))
+    key = ("batch", torch.cuda.get_device_name(dev), shapes, bool(exact), bool(per_class))
     with _LOCK:
         if key in _MEM:
             return _MEM[key]
+
+    def lx_of(shape, pol):
+        return shape[0] if pol == 0 else min(shape[0], pol)
+
     best = None
     for rows in candidates_rows:
         for pol in lx_policies:
-            lxs = [s[0] if pol == 0 else min(s[0], pol) for s in shapes]
-            trial = [replace(sp, num_steps=steps, t_final=float("inf"), fixed_dt=None,
-                             lx=lx, out=None, consume_input=False)
-                     for sp, lx in zip(specs, lxs)]
-            b = Batch(trial, rows=rows, exact=exact, autotune=False)
-            b.run()
-            st = torch.cuda.current_stream(dev)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(st)
-            b.run()
-            e1.record(st)
-            e1.synchronize()
-            ms = e0.elapsed_time(e1)
-            b.close()
-            del b
+            lxs = [lx_of(s, pol) for s in shapes]
+            ms = _time_batch(specs, rows, lxs, exact, dev, steps)
             if best is None or ms < best[0]:
                 best = (ms, rows, lxs)
-    res = (best[1], best[2])
+    ms_best, rows, lxs = best
+    if per_class:
+        classes = sorted(set(shapes), key=lambda s: -s[0] * s[1] * s[2])
+        for cls in classes:
+            members = [i for i, s in enumerate(shapes) if s == cls]
+            tried = {lxs[members[0]]}
+            for pol in lx_policies:
+                lx = lx_of(cls, pol)
+                if lx in tried:
+                    continue
+                tried.add(lx)
+                cand = list(lxs)
+                for i in members:
+                    cand[i] = lx
+                ms = _time_batch(specs, rows, cand, exact, dev, steps)
+                if ms < ms_best:
+                    ms_best, lxs = ms, cand
+    res = (rows, lxs)
     with _LOCK:
         _MEM[key] = res
     return res
