@@ -461,10 +461,46 @@ def measure_serving(torch, tg, dev, rate, requests):
             "p50_ratio": bt["p50_s"] / st["p50_s"], "p99_ratio": bt["p99_s"] / st["p99_s"]}
 
 
+def measure_batch_classes(torch, tg, dev, K=100, count=32, sizes=(32, 48, 64, 96, 128)):
+    """Per size class: a batch of `count` overpressure instances of one grid
+    size (one persistent launch, tuned) against one instance of that size
+    run alone (run_steps, tuned tile), both in Gcell-updates/s."""
+    from tinyfluids_gb300.batching import Batch, InstanceSpec
+    st = torch.cuda.current_stream(dev)
+    out = {}
+    for n in sizes:
+        specs = [InstanceSpec(*tg.overpressure(n, seed=i, device=dev), GAMMA, num_steps=K)
+                 for i in range(count)]
+        b = Batch(specs, autotune=True, capture_graph=True)
+        for _ in range(3):
+            b.run()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        b.run()
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms_b = e0.elapsed_time(e1)
+        W, dx = specs[0].state, specs[0].grid_spacing
+        for _ in range(3):
+            tg.run_steps(W, dx, GAMMA, K, tile="auto")
+        e0.record(st)
+        tg.run_steps(W, dx, GAMMA, K, tile="auto")
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms_a = e0.elapsed_time(e1)
+        out[str(n)] = {"batch_gcell_updates_per_s": count * n ** 3 * K / (ms_b * 1e-3) / 1e9,
+                       "alone_gcell_updates_per_s": n ** 3 * K / (ms_a * 1e-3) / 1e9,
+                       "instances": count, "lx": sorted({sp.lx for sp in b.specs}),
+                       "rows": b.rows}
+        b.close()
+    return out
+
+
 def run_batch_workload(args):
     torch, tg, dev = _gpu_setup()
     K = args.steps if args.steps != 200 else 100
     r = measure_batching(torch, tg, dev, args.instances, K, args.warmup)
+    r["per_size_class"] = measure_batch_classes(torch, tg, dev, K)
     line = {"metric": f"batched solves/s ({args.instances} uneven instances, {K} CFL steps each)",
             "value": r["solves_per_s"], "unit": "solves/s", "higher_is_better": True,
             "n_gpus": 1, "dtype": "f32", "data": "synthetic",
