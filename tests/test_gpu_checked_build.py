@@ -5,8 +5,8 @@ outside the state would be counted and skipped), and every stored cell
 increments a per-cell write counter, so each case below shows that the step
 touches no memory outside its buffers and writes every cell exactly once:
 no two tiles overlap in what they store and none is missed, for ragged
-shapes, all tile heights, short and long x chunks, both boundary modes, both
-arithmetic policies, and the run loop.
+shapes, both tile layouts (x- and y-marching), all tile heights, short and
+long chunks, both boundary modes, both arithmetic policies, and the run loop.
 """
 import ctypes
 
@@ -20,8 +20,10 @@ GAMMA = 5.0 / 3.0
 SHAPES = [(1, 1, 1), (2, 3, 5), (5, 7, 33), (33, 17, 61), (40, 31, 64), (3, 64, 29),
           (64, 15, 2), (31, 30, 32)]
 # (rows, lx, loader): loader 1 = per-thread loads, 2 = TMA-staged planes
-# (falls back to loads when nz % 4 != 0); the TMA path's stores are counted
-TILES = [None, (8, 3, 1), (16, 1, 1), (16, 5, 1), (32, 2, 1), (32, 7, 1), (16, 5, 2), (32, 3, 2)]
+# (falls back to loads when nz % 4 != 0; the TMA path's stores are counted),
+# 3 = the y-marching tile (lx = y planes per CTA)
+TILES = [None, (8, 3, 1), (16, 1, 1), (16, 5, 1), (32, 2, 1), (32, 7, 1), (16, 5, 2), (32, 3, 2),
+         (8, 0, 3), (8, 1, 3), (16, 2, 3)]
 
 
 @pytest.fixture(scope="module")

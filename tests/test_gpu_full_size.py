@@ -40,7 +40,7 @@ def test_cfl_dt_matches_oracle(tg, oracle_lib, shear):
 def test_tile_shapes_agree(tg, shear):
     W, dx, dt = shear
     ref = tg._evolve_state(W, dx, dt, GAMMA)
-    for tile in ((8, 64), (32, 128), (16, 7)):
+    for tile in ((8, 64), (32, 128), (16, 7), (16, 0, "ldg"), (8, 0, "ym"), (16, 64, "ym")):
         assert torch.equal(tg._evolve_state(W, dx, dt, GAMMA, tile=tile), ref), tile
 
 

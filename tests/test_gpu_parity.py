@@ -58,7 +58,7 @@ def test_exact_fused_step_bit_identical(tg, shape, hb):
     dx = 0.05
     dt = F._cfl_time_step(W, dx, GAMMA)
     ref = F._evolve_state(W, dx, dt, GAMMA, hb)
-    for tile in (None, (8, 3), (16, 1), (32, 2), (32, 5, "tma")):
+    for tile in (None, (8, 3), (16, 1), (32, 2), (32, 5, "tma"), (8, 3, "ym"), (16, 1, "ym")):
         out = host(tg._evolve_state(dev(W), dx, float(dt), GAMMA, hb, exact=True, tile=tile))
         assert np.array_equal(out, ref), (shape, hb, tile, np.abs(out - ref).max())
 
@@ -163,12 +163,73 @@ def test_fast_step_close_to_reference(tg, shape, hb):
     assert rel_err(out, ref) < FAST_STEP_RTOL
 
 
-def test_fast_step_independent_of_tile_shape(tg):
-    W = dev(random_state((70, 45, 77), 8))
+@pytest.mark.parametrize("shape", [(70, 45, 77), (37, 29, 124)])
+def test_fast_step_independent_of_tile_shape(tg, shape):
+    """Every tile layout, height and chunk length gives the same bits (odd nz:
+    the y-marching tile's 4-byte path; even nz: its 8-byte pair path)."""
+    W = dev(random_state(shape, 8))
     outs = [host(tg._evolve_state(W, 0.05, 1e-3, GAMMA, tile=t))
-            for t in (None, (16, 64), (16, 5), (8, 1), (8, 70), (32, 7), (32, 70, "tma"), (32, 1))]
+            for t in (None, (16, 64), (16, 5), (8, 1), (8, 70), (32, 7), (32, 70, "tma"), (32, 1),
+                      (8, 0, "ym"), (8, 1, "ym"), (8, 7, "ym"), (16, 0, "ym"), (16, 3, "ym"))]
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
+
+
+YM_SHAPES = [(1, 1, 1), (2, 3, 5), (5, 7, 33), (4, 9, 60), (9, 13, 62), (13, 5, 121),
+             (40, 31, 64), (3, 64, 29), (64, 15, 2), (17, 2, 130)]
+
+
+@pytest.mark.parametrize("shape", YM_SHAPES)
+@pytest.mark.parametrize("hb", [False, True])
+@pytest.mark.parametrize("exact", [False, True])
+def test_y_marching_tile_bitwise(tg, shape, hb, exact):
+    """The y-marching tile (x rows across warps, z pairs in lanes, derived
+    x halo rows, cp.async input ring) equals the x-marching tile bit for bit
+    for ragged shapes, both boundary modes, both policies and every chunk
+    length; the exact form also equals the oracle."""
+    if hb and min(shape) < 2:
+        pytest.skip("open boundaries need two cells per axis")
+    W = random_state(shape, 53)
+    dt = F._cfl_time_step(W, 0.05, GAMMA)
+    Wd = dev(W)
+    ref = tg._evolve_state(Wd, 0.05, float(dt), GAMMA, hb, exact=exact, tile=(16, 0, "ldg"))
+    for tile in ((8, 0, "ym"), (8, 1, "ym"), (8, 2, "ym"), (16, 0, "ym"), (16, 3, "ym")):
+        out = tg._evolve_state(Wd, 0.05, float(dt), GAMMA, hb, exact=exact, tile=tile)
+        assert torch.equal(out, ref), (shape, hb, exact, tile)
+    if exact:
+        assert np.array_equal(host(ref), F._evolve_state(W, 0.05, dt, GAMMA, hb))
+
+
+@pytest.mark.parametrize("shape", [(40, 31, 64), (9, 13, 62)])
+def test_y_marching_conserved_and_diagnostics(tg, shape):
+    """The conserved-in/out step (the adjoint's forward pass) and the
+    diagnostics step in the y-marching tile equal their x-marching forms."""
+    W = dev(random_state(shape, 61))
+    U = tg.conserved_state_from_primitive(W, GAMMA)
+    a = tg._evolve_state(U, 0.05, 2e-3, GAMMA, conserved=True)
+    b = tg._evolve_state(U, 0.05, 2e-3, GAMMA, conserved=True, tile=(8, 0, "ym"))
+    assert torch.equal(a, b)
+    nz = shape[2]
+    ra = tg.diagnostics.step_with_diagnostics(W, 0.05, 2e-3, GAMMA, z=nz // 2,
+                                              tile=(16, 0, "ldg"))
+    rb = tg.diagnostics.step_with_diagnostics(W, 0.05, 2e-3, GAMMA, z=nz // 2,
+                                              tile=(8, 3, "ym"))
+    assert torch.equal(ra[0], rb[0])  # the state
+    assert torch.equal(ra[2], rb[2])  # the rho / p slice
+    # the totals are summed in another order: equal to float64 rounding
+    assert torch.allclose(ra[1], rb[1], rtol=1e-10, atol=0)
+
+
+def test_y_marching_loops_match(tg):
+    """Run loops (fixed step count and the device-side t_final loop) in the
+    y-marching tile reproduce the x-marching tile's states."""
+    W, dx = tg.shear_layer(64, seed=2)
+    a = tg.run_steps(W, dx, GAMMA, 9, tile=(16, 16, "ldg"))
+    b = tg.run_steps(W, dx, GAMMA, 9, tile=(8, 16, "ym"))
+    assert torch.equal(a, b)
+    c, ic = tg.time_integration_fn(W, dx, 0.01, GAMMA, False, False, tile=(16, 0, "ldg"))
+    d, id_ = tg.time_integration_fn(W, dx, 0.01, GAMMA, False, False, tile=(8, 0, "ym"))
+    assert int(ic) == int(id_) and torch.equal(c, d)
 
 
 @pytest.mark.parametrize("shape", [(5, 7, 33), (40, 31, 64), (17, 66, 3)])
@@ -202,6 +263,8 @@ def test_fused_conserved_step_equals_conserved_sweeps(tg, shape):
         tg._evolve_state(U, 0.05, dt, GAMMA, conserved=True, exact=True)
     with pytest.raises(tg.TinyfluidsError):
         tg._evolve_state(U, 0.05, dt, GAMMA, conserved=True, tile=(8, 4))
+    with pytest.raises(tg.TinyfluidsError):
+        tg._evolve_state(U, 0.05, dt, GAMMA, tile=(32, 0, "ym"))
 
 
 @pytest.mark.parametrize("axis,shift", [(1, 3), (2, -5), (3, 31)])

@@ -80,8 +80,10 @@ def test_latency_stats():
 
 def test_autotune_candidates_and_size_classes():
     c = autotune.candidates((64, 64, 64))
-    assert (16, 0) in c and (16, 64) in c and (8, 2) in c
-    assert all(r in (8, 16, 32) and lx < 64 or lx == 64 for r, lx in c)
+    assert (16, 0, "ldg") in c and (16, 64, "ldg") in c and (8, 2, "ldg") in c
+    assert (8, 0, "ym") in c and (16, 32, "ym") in c
+    assert all(r in (8, 16, 32) and lx <= 64 for r, lx, _ in c)
+    assert all(r in (8, 16) for r, _, lay in c if lay == "ym")
     assert autotune.size_class(1) == 16 and autotune.size_class(33) == 48
     assert autotune.size_class(512) == 512 and autotune.size_class(5000) == 1024
 

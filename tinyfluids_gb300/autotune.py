@@ -1,11 +1,13 @@
 """Tile-shape autotuner for the fused step kernel.
 
-The fused kernel's tile has two free parameters (``tf_tile_config``): the tile
-height ``rows`` (8, 16 or 32 grid rows incl. the one-cell ring; the kernel
-runs rows/2 warps) and ``lx``, the number of x planes one CTA marches through.
-Taller tiles waste fewer halo rows; shorter ones let two or more CTAs share an
-SM and interleave their barrier phases; ``lx`` trades per-chunk warm-up work
-against the number of CTAs.  The best pair depends on the grid size and is
+The fused kernel has two tile layouts and, for each, two free parameters
+(``tf_tile_config``).  The x-marching tile ("ldg"): the tile height ``rows``
+(8, 16 or 32 grid rows incl. the one-cell ring; the kernel runs rows/2 warps)
+and ``lx``, the number of x planes one CTA marches through.  The y-marching
+tile ("ym"): rows/2 x rows per CTA (8 or 16 rows) and ``lx`` y planes per CTA.
+Taller tiles waste fewer halo rows; shorter ones let more CTAs share an SM and
+interleave their barrier phases; ``lx`` trades per-chunk warm-up work against
+the number of CTAs.  The best choice depends on the grid size and is
 measured, not modelled: ``tune`` times every candidate with CUDA events on the
 device and keeps the fastest.  Results are cached per (GPU, grid shape,
 arithmetic) in memory and in a JSON file (``$TINYFLUIDS_GB300_TUNE_CACHE`` or
@@ -65,16 +67,21 @@ def _save_file(data):
 
 def _key(device, shape, exact):
     name = torch.cuda.get_device_name(device).replace(" ", "_")
-    return f"{name}|{shape[0]}x{shape[1]}x{shape[2]}|{'exact' if exact else 'fast'}"
+    # v2: the y-marching tile is among the candidates
+    return f"v2|{name}|{shape[0]}x{shape[1]}x{shape[2]}|{'exact' if exact else 'fast'}"
 
 
 def candidates(shape):
-    """(rows, lx) pairs worth timing for a grid shape; lx 0 is the built-in
-    chunk-length heuristic."""
-    nx = shape[0]
+    """(rows, lx, layout) triples worth timing for a grid shape: layout "ldg"
+    is the x-marching tile (lx = x planes per CTA), "ym" the y-marching tile
+    (lx = y planes per CTA, 8 or 16 rows); lx 0 is the built-in chunk-length
+    heuristic."""
+    nx, ny = shape[0], shape[1]
     lxs = sorted({lx for lx in (2, 4, 8, 16, 32, 64, 96, 128, 192, 256, 512) if lx < nx}
                  | {nx, 0})
-    return [(r, lx) for r in ROWS for lx in lxs]
+    lys = sorted({ly for ly in (8, 16, 32, 64, 128) if ly < ny} | {0})
+    return ([(r, lx, "ldg") for r in ROWS for lx in lxs] +
+            [(r, ly, "ym") for r in (8, 16) for ly in lys])
 
 
 def _time_config(W, dx, tile, exact, reps, steps):
@@ -114,11 +121,13 @@ def tune(shape, exact=False, device=None, reps=3, steps=3, force=False, persist=
     W = W_full[:, :shape[0], :shape[1], :shape[2]].contiguous()
     del W_full
     table = {}
-    for rows, lx in candidates(shape):
-        table[f"{rows},{lx}"] = _time_config(W, dx, (rows, lx), exact, reps, steps)
+    for rows, lx, layout in candidates(shape):
+        table[f"{rows},{lx},{layout}"] = _time_config(W, dx, (rows, lx, layout), exact, reps,
+                                                      steps)
     best = min(table, key=table.get)
-    rows, lx = (int(v) for v in best.split(","))
-    res = {"rows": rows, "lx": lx, "ms": table[best], "table": table}
+    rows, lx, layout = best.split(",")
+    res = {"rows": int(rows), "lx": int(lx), "layout": layout, "ms": table[best],
+           "table": table}
     with _LOCK:
         _MEM[key] = res
         if persist:
@@ -129,9 +138,9 @@ def tune(shape, exact=False, device=None, reps=3, steps=3, force=False, persist=
 
 
 def tuned_tile(shape, exact=False, device=None):
-    """(rows, lx) from the cache (tuning on first use)."""
+    """(rows, lx, layout) from the cache (tuning on first use)."""
     r = tune(shape, exact=exact, device=device)
-    return r["rows"], r["lx"]
+    return r["rows"], r["lx"], r.get("layout", "ldg")
 
 
 def size_class(n: int) -> int:

@@ -44,6 +44,7 @@ struct FusedGeom {
   int tiles_z, tiles_y, tiles_x;  // tile grid
   int lx;                         // planes per x chunk
   int open_bc;                    // TF_FLAG_OPEN_BOUNDARIES set
+  int pairs8;  // y-marching tile: source and destination rows move z pairs as 8-byte units
 };
 
 // Per-variable base pointers of a launch's source and destination states

@@ -29,6 +29,15 @@ struct Cell2 {
 __device__ __forceinline__ V2 v2(float x, float y) { return make_float2(x, y); }
 __device__ __forceinline__ V2 splat(float x) { return make_float2(x, x); }
 
+// Accessor view of a Cell2 in registers (the left cell of hll_from).
+struct CellRef2 {
+  const Cell2& c;
+  __device__ __forceinline__ V2 wa() const { return c.wa; }
+  __device__ __forceinline__ V2 wb() const { return c.wb; }
+  __device__ __forceinline__ V2 U(int i) const { return c.U[i]; }
+  __device__ __forceinline__ V2 F(int i) const { return c.F[i]; }
+};
+
 // ---------------------------------------------------------------------------
 // FastPair
 // ---------------------------------------------------------------------------
@@ -77,13 +86,20 @@ struct FastPair {
 
   // FastPolicy::hll on both cells
   static __device__ __forceinline__ void hll(const Cell2& L, const Cell2& R, V2 F[5]) {
-    V2 sp = vmax(vmax(L.wa, R.wa), splat(0.f));
-    V2 ns = vmax(vmax(L.wb, R.wb), splat(0.f));
+    hll_from(CellRef2{L}, CellRef2{R}, F);
+  }
+  // The same, with the cells read through accessors (wa(), wb(), U(i), F(i))
+  // at the point of use -- for cells held in shared memory or in another
+  // lane, so that their values need registers only briefly.
+  template <class LC, class RC>
+  static __device__ __forceinline__ void hll_from(const LC& L, const RC& R, V2 F[5]) {
+    V2 sp = vmax(vmax(L.wa(), R.wa()), splat(0.f));
+    V2 ns = vmax(vmax(L.wb(), R.wb()), splat(0.f));
     V2 inv = rcp(add(sp, ns));
     V2 a = mul(sp, inv), b = mul(ns, inv);
     V2 s = mul(ns, a);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) F[i] = fma(a, L.F[i], fma(b, R.F[i], mul(s, sub(L.U[i], R.U[i]))));
+    for (int i = 0; i < 5; ++i) F[i] = fma(a, L.F(i), fma(b, R.F(i), mul(s, sub(L.U(i), R.U(i)))));
   }
 
   static __device__ __forceinline__ void update(const Cell2& C, const V2 flo[5], const V2 fhi[5],
@@ -182,6 +198,22 @@ struct ExactPair {
     E::hll(lo(L), lo(R), fa);
     E::hll(hi(L), hi(R), fb);
     merge(F, fa, fb);
+  }
+  template <class LC, class RC>
+  static __device__ __forceinline__ void hll_from(const LC& L, const RC& R, V2 F[5]) {
+    Cell2 l, r;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      l.U[i] = L.U(i);
+      l.F[i] = L.F(i);
+      r.U[i] = R.U(i);
+      r.F[i] = R.F(i);
+    }
+    l.wa = L.wa();
+    l.wb = L.wb();
+    r.wa = R.wa();
+    r.wb = R.wb();
+    hll(l, r, F);
   }
   static __device__ __forceinline__ void update(const Cell2& C, const V2 flo[5], const V2 fhi[5],
                                                 V2 s_out[5], const StepConsts<float>& k) {

@@ -10,6 +10,7 @@
 
 #include "tf_common.cuh"
 #include "tf_fused.cuh"
+#include "tf_fused_ym.cuh"
 #include "tf_host.h"
 #include "tf_math.cuh"
 
@@ -314,6 +315,7 @@ struct FusedArgs {
   double* totals;  // diagnostics instantiation: conserved totals (zeroed before)
   DiagArgs diag;   // diagnostics instantiation: optional slice
   int conserved_io;  // fast policy on conserved input and output (16-row tiles)
+  int layout;        // 0: x-marching tile (fused_tile), 1: y-marching tile (fused_tile_ym)
 };
 
 // dt of a launch: a loop step reads the loop's dt (or its fixed dt) and runs
@@ -350,6 +352,28 @@ __global__ void TF_FUSED_BOUNDS(NWP) fused_step_kernel(const __grid_constant__ F
   const StepConsts<float> K = launch_consts(a, dt);
   CSum acc[5];
   float m = fused_tile<P, NWP, false, DIAG, VP && !DIAG && !P::kExact>(a.src, a.dst, a.geo, blockIdx.x, blockIdx.y,
+                                                blockIdx.z, K, sm, a.diag, acc, &a.vp);
+  if constexpr (DIAG) block_add_totals(acc, dred, a.totals);
+  if (a.ctl) {
+    float bm = block_max(m, sm.red);
+    if (threadIdx.x == 0)
+      ctl_finish_cta(a.ctl, bm, gridDim.x * gridDim.y * gridDim.z, dt, a.loop != 0);
+  }
+}
+
+// The y-marching fused step (fused_tile_ym): NW x rows per CTA, grid
+// (x tiles, z tiles, y chunks).
+template <class P, int NW, bool DIAG = false, bool VP = false, bool VEC = false>
+__global__ void __launch_bounds__(NW * 32, min_ctas_per_sm(NW))
+    fused_step_ym_kernel(const __grid_constant__ FusedArgs a) {
+  extern __shared__ __align__(16) unsigned char ym_smem[];
+  YmSmem<NW>& sm = *reinterpret_cast<YmSmem<NW>*>(ym_smem);
+  __shared__ double dred[DIAG ? NW * 5 : 1];
+  float dt;
+  if (!launch_dt(a, &dt)) return;
+  const StepConsts<float> K = launch_consts(a, dt);
+  CSum acc[5];
+  float m = fused_tile_ym<P, NW, DIAG, VP, VEC>(a.src, a.dst, a.geo, blockIdx.x, blockIdx.y,
                                                 blockIdx.z, K, sm, a.diag, acc, &a.vp);
   if constexpr (DIAG) block_add_totals(acc, dred, a.totals);
   if (a.ctl) {
@@ -443,12 +467,48 @@ static int check_scalars(float dx, float gamma) {
   return TF_OK;
 }
 
-static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int lx) {
+// Tile grid of a fused step.  layout 0 (x-marching): tiles_z x tiles_y tiles
+// of 30 x (rows-2) stored cells, marching along x in chunks of lx planes.
+// layout 1 (y-marching): tiles_x x tiles_z tiles of rows/2 x rows and 62 z
+// cells, marching along y in chunks of lx planes (tiles_y chunks); the chunk
+// rule is the same with the axes' roles exchanged.
+static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int lx,
+                           int layout = 0) {
   FusedGeom g;
   g.nx = nx;
   g.ny = ny;
   g.nz = nz;
   g.open_bc = (flags & TF_FLAG_OPEN_BOUNDARIES) ? 1 : 0;
+  if (layout == 1) {
+    const int nw = rows / 2;
+    g.tiles_x = (nx + nw - 1) / nw;
+    g.tiles_z = (nz + kYmZ - 1) / kYmZ;
+    if (lx <= 0) {
+      const long long tiles_xz = (long long)g.tiles_x * g.tiles_z;
+      const long long resident = (long long)sm_count() * min_ctas_per_sm(nw);
+      long long min_planes;
+      if (tiles_xz * (ny / 16) >= resident) {
+        min_planes = 16;
+      } else if (tiles_xz * (ny / 8) >= resident) {
+        min_planes = 8;
+      } else {
+        min_planes = (ny * tiles_xz + resident - 1) / resident;
+        if (min_planes < 2) min_planes = 2;
+      }
+      // about 9 waves, and chunks of at most 64 planes (measured at 512^3 to
+      // 1024^3: 32-64 planes beat longer chunks by 2-7%)
+      long long ty = (9 * resident + tiles_xz - 1) / tiles_xz;
+      if (ty < (ny + 63) / 64) ty = (ny + 63) / 64;
+      long long max_ty = ny / min_planes > 0 ? ny / min_planes : 1;
+      if (ty > max_ty) ty = max_ty;
+      if (ty < 1) ty = 1;
+      lx = (int)((ny + ty - 1) / ty);
+    }
+    if (lx > ny) lx = ny;
+    g.lx = lx;
+    g.tiles_y = (ny + lx - 1) / lx;
+    return g;
+  }
   g.tiles_z = (nz + kTileZ - 1) / kTileZ;
   g.tiles_y = (ny + (rows - 2) - 1) / (rows - 2);
   if (lx <= 0) {
@@ -482,8 +542,30 @@ static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int
   return g;
 }
 
-static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx, int* loader) {
-  *rows = 16;  // two CTAs per SM interleave their barrier phases (measured best at 512^3)
+// Fraction of extra cells a layout computes for a grid (ring and ragged
+// tiles): the x-marching 16-row tile stores 30 x 14 of 32 x 16 cells; the
+// y-marching 8-row tile stores 60 of 64 z cells and derives two halo rows per
+// 4 rows (about 7.8% more arithmetic, measured on the FP32 pipe counters).
+static double overlap_xmarch(int ny, int nz) {
+  const double y = (double)((ny + 13) / 14) * 16 / ny;
+  const double z = (double)((nz + kTileZ - 1) / kTileZ) * kTileLanes / nz;
+  return y * z;
+}
+static double overlap_ymarch(int nz) {
+  return (double)((nz + kYmZ - 1) / kYmZ) * 64 / nz * 1.078;
+}
+
+// The tile of a fused step.  With no tile given, the fast and diagnostics
+// steps on a periodic grid with an even nz and at least 4 x rows take the
+// y-marching 8-row tile when it computes at least 7% fewer cells than the
+// x-marching 16-row tile (measured on GB300: 86-87 against 83-84
+// Gcell-updates/s for the 512^3 shear layer; within 2% of each other at 384^3
+// and 768^3 and slower below 384^3, where the rule keeps the x-marching tile);
+// otherwise the x-marching 16-row tile (two CTAs per SM interleave their
+// barrier phases).  loader 3 selects the y-marching tile explicitly.
+static int resolve_tile(const tf_tile_config* tile, int nx, int ny, int nz, unsigned flags,
+                        int* rows, int* lx, int* loader) {
+  *rows = 16;
   *lx = 0;
   *loader = 0;
   if (tile) {
@@ -492,9 +574,19 @@ static int resolve_tile(const tf_tile_config* tile, int* rows, int* lx, int* loa
     *rows = tile->rows;
     *lx = tile->lx;
     if (*lx < 0) return set_error(TF_ERR_ARG, "tile lx must be >= 0");
-    if (tile->loader < 0 || tile->loader > 2)
-      return set_error(TF_ERR_ARG, "tile loader must be 0 (auto), 1 (loads) or 2 (TMA)");
+    if (tile->loader < 0 || tile->loader > 3)
+      return set_error(TF_ERR_ARG,
+                       "tile loader must be 0 (auto), 1 (loads), 2 (TMA) or 3 (y-marching)");
+    if (tile->loader == 3 && tile->rows == 32)
+      return set_error(TF_ERR_ARG, "the y-marching tile takes 8 or 16 rows");
     *loader = tile->loader;
+    return TF_OK;
+  }
+  const bool fit = !(flags & (TF_FLAG_EXACT | TF_FLAG_OPEN_BOUNDARIES)) && (nz & 1) == 0 &&
+                   nx >= 4;
+  if (fit && overlap_xmarch(ny, nz) >= 1.07 * overlap_ymarch(nz)) {
+    *rows = 8;
+    *loader = 3;
   }
   return TF_OK;
 }
@@ -511,6 +603,35 @@ static int launch_tma(const FusedArgs& a, dim3 grid, const CUtensorMap& tm, bool
   return TF_OK;
 }
 
+// Template arguments of one y-marching kernel instantiation.
+template <class P_, int NW_, bool DIAG_, bool VP_, bool VEC_ = false>
+struct YmTag {
+  using P = P_;
+  static constexpr int nw = NW_;
+  static constexpr bool diag = DIAG_, vp = VP_, vec = VEC_;
+};
+
+// Dynamic shared memory of the y-marching kernel with NW warps.
+static size_t ym_smem_bytes(int nw) {
+  return nw == 4 ? sizeof(YmSmem<4>) : sizeof(YmSmem<8>);
+}
+
+// Raises a kernel's dynamic shared-memory limit once per device (the flag
+// is per kernel instantiation: Tag is the kernel's template arguments).
+template <class Tag, class Kern>
+static int ym_smem_attr(Kern kern, size_t bytes) {
+  static std::atomic<unsigned long long> done{0};
+  int dev = 0;
+  TF_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load() & bit) return TF_OK;
+  TF_TRY(cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bytes),
+                    "cudaFuncSetAttribute"));
+  done.fetch_or(bit);
+  return TF_OK;
+}
+
 // Launches one fused step.  loader: 0 auto, 1 per-thread loads, 2 TMA-staged
 // planes (falls back to loads when not usable).  Auto takes the per-thread
 // loads: on GB300 at 256^3-512^3 they measured faster (80 vs 64 Gcell/s at
@@ -524,6 +645,47 @@ static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_
   for (int i = 0; i < 5; ++i) {
     a.vp.s[i] = a.src + i * vs;
     a.vp.d[i] = a.dst ? a.dst + i * vs : nullptr;
+  }
+  if (a.layout == 1) {
+    if (a.geo.tiles_z > 65535) return set_error(TF_ERR_ARG, "grid too large for the tile grid");
+    a.geo.pairs8 = ((reinterpret_cast<uintptr_t>(a.src) | reinterpret_cast<uintptr_t>(a.dst)) &
+                    7) == 0 && (vs & 1) == 0 && (a.geo.nz & 1) == 0;
+    const dim3 g(a.geo.tiles_x, a.geo.tiles_z, a.geo.tiles_y);
+    const bool vp = vs < (1ull << 31);
+    // 8-byte pair accesses: periodic wrap keeps every pair whole when nz is even
+    const bool vec = a.geo.pairs8 && !a.geo.open_bc;
+    int st = TF_OK;
+    auto go = [&](auto nw_c) {
+      constexpr int NW = decltype(nw_c)::value;
+      auto launch = [&](auto tag) {
+        using T = decltype(tag);
+        auto kern = fused_step_ym_kernel<typename T::P, NW, T::diag, T::vp, T::vec>;
+        const size_t smem = ym_smem_bytes(NW);
+        st = ym_smem_attr<T>(kern, smem);
+        if (st == TF_OK) kern<<<g, NW * 32, smem, s>>>(a);
+      };
+      if (a.totals) {
+        if (exact) launch(YmTag<ExactPair, NW, true, false>{});
+        else launch(YmTag<FastPair, NW, true, false>{});
+      } else if (a.conserved_io) {
+        if (vp && vec) launch(YmTag<FastPairConserved, NW, false, true, true>{});
+        else if (vp) launch(YmTag<FastPairConserved, NW, false, true>{});
+        else launch(YmTag<FastPairConserved, NW, false, false>{});
+      } else if (exact) {
+        launch(YmTag<ExactPair, NW, false, false>{});
+      } else if (vp && vec) {
+        launch(YmTag<FastPair, NW, false, true, true>{});
+      } else if (vp) {
+        launch(YmTag<FastPair, NW, false, true>{});
+      } else {
+        launch(YmTag<FastPair, NW, false, false>{});
+      }
+    };
+    if (rows == 8) go(std::integral_constant<int, 4>{});
+    else if (rows == 16) go(std::integral_constant<int, 8>{});
+    else return set_error(TF_ERR_ARG, "the y-marching tile takes 8 or 16 rows");
+    TF_TRY(st);
+    return launch_check("fused_step_ym_kernel");
   }
   dim3 grid(a.geo.tiles_z, a.geo.tiles_y, a.geo.tiles_x);
   if (loader == 2 && tma_usable(a, rows)) {
@@ -925,9 +1087,10 @@ int tf_evolve_state(const float* W_in, float* W_out, int nx, int ny, int nz, flo
   TF_TRY(check_scalars(dx, gamma));
   if (!dt_dev && !isfinite(dt_host)) return set_error(TF_ERR_ARG, "dt must be finite");
   int rows, lx, loader;
-  TF_TRY(resolve_tile(tile, &rows, &lx, &loader));
-  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
+  TF_TRY(resolve_tile(tile, nx, ny, nz, flags, &rows, &lx, &loader));
+  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx, loader == 3 ? 1 : 0);
   FusedArgs a = make_fused_args(W_in, W_out, geo, dx, gamma);
+  a.layout = loader == 3 ? 1 : 0;
   a.dt_host = dt_host;
   a.dt_dev = dt_dev;
   a.loop = 0;
@@ -937,7 +1100,7 @@ int tf_evolve_state(const float* W_in, float* W_out, int nx, int ny, int nz, flo
     if ((flags & cons) != cons)
       return set_error(TF_ERR_UNSUPPORTED, "the fused step takes conserved input and output together");
     a.conserved_io = 1;
-    loader = 1;
+    if (loader != 3) loader = 1;
   }
   return launch_fused(a, rows, (flags & TF_FLAG_EXACT) != 0, (cudaStream_t)stream, loader);
 }
@@ -954,9 +1117,10 @@ int tf_evolve_state_diag(const float* W_in, float* W_out, int nx, int ny, int nz
   if (slice && (z_slice < 0 || z_slice >= nz))
     return set_error(TF_ERR_ARG, "z_slice %d outside [0, %d)", z_slice, nz);
   int rows, lx, loader;
-  TF_TRY(resolve_tile(tile, &rows, &lx, &loader));
-  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
+  TF_TRY(resolve_tile(tile, nx, ny, nz, flags, &rows, &lx, &loader));
+  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx, loader == 3 ? 1 : 0);
   FusedArgs a = make_fused_args(W_in, W_out, geo, dx, gamma);
+  a.layout = loader == 3 ? 1 : 0;
   a.dt_host = dt_host;
   a.dt_dev = dt_dev;
   a.loop = 0;
@@ -1036,7 +1200,7 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
   if (max_steps < 0 && !isfinite(t_final))
     return set_error(TF_ERR_ARG, "an unbounded loop needs a finite t_final or max_steps >= 0");
   int rows, lx, loader;
-  TF_TRY(resolve_tile(tile, &rows, &lx, &loader));
+  TF_TRY(resolve_tile(tile, nx, ny, nz, flags, &rows, &lx, &loader));
   cudaStream_t s = (cudaStream_t)stream;
   const long long n = (long long)nx * ny * nz;
   const bool exact = (flags & TF_FLAG_EXACT) != 0;
@@ -1045,7 +1209,7 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
   maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W_in, n, gamma, ctl, exact ? 0 : 1);
   TF_TRY(launch_check("maxspeed_kernel"));
 
-  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
+  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx, loader == 3 ? 1 : 0);
   // with a known step count, choose the ping-pong roles so that the last
   // step writes W_out (step i writes buf[i & 1], i = 1..max_steps)
   float* b0 = work;
@@ -1055,6 +1219,7 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
     b1 = work;
   }
   FusedArgs a = make_fused_args(W_in, nullptr, geo, dx, gamma);
+  a.layout = loader == 3 ? 1 : 0;
   a.loop = 1;
   a.ctl = ctl;
   a.fixed_dt = fixed_dt;
@@ -1247,12 +1412,12 @@ extern "C" int tf_time_integration_noalloc(const float* W_in, float* W_out, int 
   const bool exact = (flags & TF_FLAG_EXACT) != 0;
   // the tile of tf_time_integration's default (16 rows, heuristic chunk length)
   int rows, lx, loader;
-  TF_TRY(resolve_tile(nullptr, &rows, &lx, &loader));
+  TF_TRY(resolve_tile(nullptr, nx, ny, nz, flags, &rows, &lx, &loader));
   // the control block keeps the previous call's contents: re-initialise all of it
   ctl_init_kernel<<<1, 1, 0, s>>>(ctl, t_final, cfl * dx, max_steps);
   maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W_in, n, gamma, ctl, exact ? 0 : 1);
   TF_TRY(launch_check("maxspeed_kernel"));
-  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx);
+  FusedGeom geo = make_geom(nx, ny, nz, flags, rows, lx, loader == 3 ? 1 : 0);
   float* b0 = work;
   float* b1 = W_out;
   if (max_steps >= 0 && (max_steps & 1) == 0) {
@@ -1260,6 +1425,7 @@ extern "C" int tf_time_integration_noalloc(const float* W_in, float* W_out, int 
     b1 = work;
   }
   FusedArgs a = make_fused_args(W_in, nullptr, geo, dx, gamma);
+  a.layout = loader == 3 ? 1 : 0;
   a.loop = 1;
   a.ctl = ctl;
   a.fixed_dt = fixed_dt;

@@ -310,9 +310,10 @@ def _evolve_state_along_axis(primitive_state, grid_spacing, dt, gamma, axis, *,
 
 
 def _tile_arg(tile, state=None, exact=None):
-    """tf_tile_config for `tile`: None (built-in heuristic), (rows, lx),
-    (rows, lx, loader) with loader "auto" | "ldg" | "tma", or "auto" (the
-    autotuner's measured best for this grid shape)."""
+    """tf_tile_config for `tile`: None (built-in choice), (rows, lx),
+    (rows, lx, loader) with loader "auto" | "ldg" | "tma" (x-marching tile)
+    or "ym" (y-marching tile, 8 or 16 rows), or "auto" (the autotuner's
+    measured best for this grid shape)."""
     if tile is None:
         return None
     if isinstance(tile, str):
@@ -322,5 +323,5 @@ def _tile_arg(tile, state=None, exact=None):
         ex = _EXACT if exact is None else bool(exact)
         tile = autotune.tuned_tile(tuple(state.shape[1:]), exact=ex, device=state.device)
     rows, lx, *rest = tile
-    loader = {"auto": 0, "ldg": 1, "tma": 2}.get(rest[0], rest[0]) if rest else 0
+    loader = {"auto": 0, "ldg": 1, "tma": 2, "ym": 3}.get(rest[0], rest[0]) if rest else 0
     return ctypes.byref(_lib.TileConfig(int(rows), int(lx), int(loader)))
