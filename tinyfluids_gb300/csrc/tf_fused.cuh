@@ -176,9 +176,7 @@ __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, 
   // the flux at x+1/2 (the caller copies them into cur / fm for the next plane)
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
-  V2 s[5];
-  P::to_state(pf, s, K);
-  P::template derive<1>(s, nxt, K);
+  P::template derive_in<1>(pf, nxt, K);
   consumed();
   P::hll(cur, nxt, fp);  // face x + 1/2
   V2 s1[5];
@@ -373,14 +371,12 @@ __device__ __forceinline__ float fused_tile(const float* __restrict__ src, float
   V2 f0[5], f1[5];
   V2 pa[5], pb[5];
   {
-    V2 w0[5], s[5];
+    V2 w0[5];
     load(t.x0 - 1, w0);
     load(t.x0, pa);
     load(t.x0 + 1, pb);
-    P::to_state(w0, s, K);
-    P::template derive<1>(s, c1, K);
-    P::to_state(pa, s, K);
-    P::template derive<1>(s, c0, K);
+    P::template derive_in<1>(w0, c1, K);
+    P::template derive_in<1>(pa, c0, K);
     if (!kAlt && t.x0 + 2 <= t.x_end) load(t.x0 + 2, pa);
     P::hll(c1, c0, f0);  // flux at face x0 - 1/2; c0 = plane x0
   }
@@ -572,13 +568,11 @@ __device__ __forceinline__ float fused_tile_tma(const float* __restrict__ src,
   Cell2 c0, c1;  // carried plane quantities, alternating roles
   V2 f0[5], f1[5];
   {
-    V2 w0[5], w1[5], s[5];
+    V2 w0[5], w1[5];
     read(0, w0);
     read(1, w1);
-    P::to_state(w0, s, K);
-    P::template derive<1>(s, c1, K);
-    P::to_state(w1, s, K);
-    P::template derive<1>(s, c0, K);
+    P::template derive_in<1>(w0, c1, K);
+    P::template derive_in<1>(w1, c0, K);
     P::hll(c1, c0, f0);  // flux at face x0 - 1/2; c0 = plane x0
   }
   if (__syncthreads_or(bad)) {

@@ -258,10 +258,9 @@ __device__ __forceinline__ float fused_tile_ym(const float* __restrict__ src,
     wait_plane();
     Cell2 cx;
     {
-      V2 in[5], s[5];
+      V2 in[5];
       read(y, false, in);
-      P::to_state(in, s, K);
-      P::template derive<1>(s, cx, K);
+      P::template derive_in<1>(in, cx, K);
     }
     ym_put_cell(sm, w, lane, cx);
     // the halo warps solve their tile-edge face before the barrier, so the
@@ -269,11 +268,10 @@ __device__ __forceinline__ float fused_tile_ym(const float* __restrict__ src,
     // to other warps through shared memory measured slower)
     V2 fxm[5], fxp[5];
     if (halo_warp) {
-      V2 hin[5], hst[5];
+      V2 hin[5];
       Cell2 hc;
       read(y, true, hin);
-      P::to_state(hin, hst, K);
-      P::template derive<1>(hst, hc, K);
+      P::template derive_in<1>(hin, hc, K);
       if (w == 0) P::hll(hc, cx, fxm);
       else P::hll(cx, hc, fxp);
     }
@@ -389,13 +387,15 @@ __device__ __forceinline__ float fused_tile_ym(const float* __restrict__ src,
     P::template derive<2>(s1, c0, K);
     P::hll(c1, c0, f0);  // c0 = plane y0, f0 = face y0 - 1/2
   }
-  // one plane per trip and the carry copied back: the two-plane form whose
-  // carried quantities alternate without copies spills registers here
-  for (int y = y0; y < y_end; ++y) {
+  // two planes per trip: the face fluxes alternate between f0 and f1, the
+  // carried cell is copied back (alternating it too spills registers here)
+  for (int y = y0; y < y_end; y += 2) {
     plane(y, c0, f0, c1, f1);
     c0 = c1;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) f0[i] = f1[i];
+    if (y + 1 < y_end) {
+      plane(y + 1, c0, f1, c1, f0);
+      c0 = c1;
+    }
   }
 #if !TF_CHECKED
   cp_async_wait_all();

@@ -181,6 +181,13 @@ struct ExactPolicy {
     o.wb = exact_sound(rho, p, k.g);
   }
 
+  // derive() of an input cell: the state is primitive, like the input
+  template <int VEL>
+  static __device__ __forceinline__ void derive_in(const T w[5], Cell<T>& o,
+                                                   const StepConsts<T>& k) {
+    derive<VEL>(w, o, k);
+  }
+
   // fluid.py:282-303
   static __device__ __forceinline__ void hll(const Cell<T>& L, const Cell<T>& R, T F[5]) {
     using O = IEEE<T>;
@@ -275,6 +282,25 @@ struct FastPolicy {
     o.F[4] = (U[4] + p) * ud;
     o.F[VEL] = fmaf(U[VEL], ud, p);
     const float c = sqrt_(k.g * p * ir);
+    o.wa = ud + c;
+    o.wb = c - ud;
+  }
+
+  // derive() of a PRIMITIVE input cell (the first sweep of a step): U is
+  // to_state(w), and the normal velocity and the pressure are the input's own
+  // (no reconstruction from U).
+  template <int VEL>
+  static __device__ __forceinline__ void derive_in(const float w[5], Cell<float>& o,
+                                                   const StepConsts<float>& k) {
+    to_state(w, o.U, k);
+    const float ud = w[VEL], p = w[4];
+    o.F[0] = o.U[VEL];
+    o.F[1] = o.U[1] * ud;
+    o.F[2] = o.U[2] * ud;
+    o.F[3] = o.U[3] * ud;
+    o.F[4] = (o.U[4] + p) * ud;
+    o.F[VEL] = fmaf(o.U[VEL], ud, p);
+    const float c = sqrt_(k.g * p * rcp(w[0]));
     o.wa = ud + c;
     o.wb = c - ud;
   }

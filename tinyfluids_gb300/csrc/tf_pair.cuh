@@ -84,6 +84,23 @@ struct FastPair {
     o.wb = sub(c, ud);
   }
 
+  // FastPolicy::derive_in on both cells (primitive input)
+  template <int VEL>
+  static __device__ __forceinline__ void derive_in(const V2 w[5], Cell2& o,
+                                                   const StepConsts<float>& k) {
+    to_state(w, o.U, k);
+    const V2 ud = w[VEL], p = w[4];
+    o.F[0] = o.U[VEL];
+    o.F[1] = mul(o.U[1], ud);
+    o.F[2] = mul(o.U[2], ud);
+    o.F[3] = mul(o.U[3], ud);
+    o.F[4] = mul(add(o.U[4], p), ud);
+    o.F[VEL] = fma(o.U[VEL], ud, p);
+    const V2 c = sqrt_(mul(mul(splat(k.g), p), rcp(w[0])));
+    o.wa = add(ud, c);
+    o.wb = sub(c, ud);
+  }
+
   // FastPolicy::hll on both cells
   static __device__ __forceinline__ void hll(const Cell2& L, const Cell2& R, V2 F[5]) {
     hll_from(CellRef2{L}, CellRef2{R}, F);
@@ -135,6 +152,11 @@ struct FastPairConserved : FastPair {
 #pragma unroll
     for (int i = 0; i < 5; ++i) U[i] = w[i];
   }
+  template <int VEL>
+  static __device__ __forceinline__ void derive_in(const V2 U[5], Cell2& o,
+                                                   const StepConsts<float>& k) {
+    FastPair::derive<VEL>(U, o, k);
+  }
   static __device__ __forceinline__ V2 finish(const V2 U[5], V2 w[5], const StepConsts<float>&) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) w[i] = U[i];
@@ -183,6 +205,11 @@ struct ExactPair {
   static __device__ __forceinline__ void to_state(const V2 w[5], V2 U[5], const StepConsts<float>&) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) U[i] = w[i];
+  }
+  template <int VEL>
+  static __device__ __forceinline__ void derive_in(const V2 s[5], Cell2& o,
+                                                   const StepConsts<float>& k) {
+    derive<VEL>(s, o, k);
   }
   template <int VEL>
   static __device__ __forceinline__ void derive(const V2 s[5], Cell2& o, const StepConsts<float>& k) {

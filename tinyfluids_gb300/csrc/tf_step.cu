@@ -930,15 +930,11 @@ __global__ void __launch_bounds__(256) sweep_kernel(const float* __restrict__ sr
       if (VEL == 3) zz += d;
       long long j = ((long long)src_index(xx, nx, open) * ny + src_index(yy, ny, open)) * nz +
                     src_index(zz, nz, open);
-      float w[5], s[5];
+      float w[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) w[v] = __ldg(src + v * n + j);
-      if (in_prim) P::to_state(w, s, K);
-      else {
-#pragma unroll
-        for (int v = 0; v < 5; ++v) s[v] = w[v];
-      }
-      P::template derive<VEL>(s, c[d + 1], K);
+      if (in_prim) P::template derive_in<VEL>(w, c[d + 1], K);
+      else P::template derive<VEL>(w, c[d + 1], K);
     }
     float flo[5], fhi[5], s[5], o[5];
     P::hll(c[0], c[1], flo);
@@ -983,15 +979,11 @@ __global__ void __launch_bounds__(256) march_sweep_kernel(const float* __restric
     const int as = src_index(a, na, open);
     const long long j = VEL == 1 ? ((long long)as * ny + os) * nz + zs
                                  : ((long long)os * ny + as) * nz + zs;
-    float w[5], st[5];
+    float w[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) w[v] = __ldg(src + v * n + j);
-    if (in_prim) P::to_state(w, st, K);
-    else {
-#pragma unroll
-      for (int v = 0; v < 5; ++v) st[v] = w[v];
-    }
-    P::template derive<VEL>(st, c, K);
+    if (in_prim) P::template derive_in<VEL>(w, c, K);
+    else P::template derive<VEL>(w, c, K);
   };
   Cell<float> prev, cur, next;
   float flo[5], fhi[5];
