@@ -220,7 +220,8 @@ def run_gpu(args):
     tg._lib.load()
     if args.exact:
         tg.set_exact(True)
-    tile = tuple(int(x) for x in args.tile.split(",")) if args.tile else None
+    tile = (tuple(int(x) if x.isdigit() else x for x in args.tile.split(","))
+            if args.tile else None)
 
     n, K, Wu = args.n, args.steps, args.warmup
     W, dx = tg.shear_layer(n, seed=rank, device=dev)
@@ -305,6 +306,11 @@ def run_gpu(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     per_launch_ms = kernel_ms
+    rt = tg.resolved_tile((n, n, n), exact=args.exact, tile=tile)
+    kernel_label = ("fused_step_ym_kernel (y-marching tile, %d x rows per CTA, %d y planes per "
+                    "CTA)" % (rt[0] // 2, rt[1]) if rt[2] == "ym" else
+                    "fused_step_kernel (x-marching tile, %d rows, %d x planes per CTA)"
+                    % (rt[0], rt[1])) + "; 40 B/cell algorithmic"
     achieved = BYTES_PER_CELL * cells / (per_launch_ms * 1e-3) / 1e9
     traffic = None
     prof = os.path.join(ROOT, "profiles", "fused_step_traffic.json")
@@ -331,7 +337,7 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_src,
-                     "kernel": "fused_step_kernel (40 B/cell algorithmic)",
+                     "kernel": kernel_label,
                      "launch_ms": per_launch_ms,
                      "launch_ms_definition": f"(time of {K} steps - time of {Kh} steps) / "
                                              f"{K - Kh}, CUDA events on the launching stream"},

@@ -72,15 +72,28 @@ typedef struct tf_ctl {
   int reserved[5];
 } tf_ctl;
 
-/* Tile shape of the fused step kernel; NULL = built-in heuristic (16 rows;
- * lx for about nine waves of resident CTAs in chunks of >= 16 planes, shorter
- * chunks for grids that would not fill one wave). */
+/* Tile of the fused step kernel; NULL = built-in choice: the y-marching
+ * 8-row tile for a fast (or diagnostics / conserved) step on a periodic grid
+ * with an even nz where it computes no more cells than the x-marching tile,
+ * else the x-marching 16-row tile; the chunk length (lx) for about nine waves
+ * of resident CTAs in chunks of >= 16 planes (y-marching: <= 64), shorter
+ * chunks for grids that would not fill one wave.  tf_resolve_tile reports the
+ * choice. */
 typedef struct tf_tile_config {
-  int rows;    /* grid rows per tile incl. the 1-cell ring: 8, 16 or 32 (rows/2 warps) */
-  int lx;      /* x planes per CTA (>= 1; 0 = heuristic) */
-  int loader;  /* 0 = auto (per-thread loads), 1 = per-thread loads, 2 = TMA-staged planes
-                  (needs nz % 4 == 0 and 16-byte aligned states; falls back otherwise) */
+  int rows;    /* x-marching: grid rows (y) per tile incl. the 1-cell ring: 8, 16 or 32
+                  (rows/2 warps); y-marching: 8 or 16 (rows/2 x rows per CTA, one warp each) */
+  int lx;      /* planes per CTA along the marching axis (x or y; >= 1; 0 = heuristic) */
+  int loader;  /* 0 = auto (x-marching, per-thread loads), 1 = x-marching with per-thread
+                  loads, 2 = x-marching with TMA-staged planes (needs nz % 4 == 0 and 16-byte
+                  aligned states; falls back otherwise), 3 = the y-marching tile (x rows
+                  across warps, z pairs per lane, input by cp.async) */
 } tf_tile_config;
+
+/* The tile a fused step with these dimensions and flags runs (tile NULL: the
+ * built-in choice), written to *out with lx resolved; no counterpart in the
+ * reference (introspection of this library's tiling). */
+int tf_resolve_tile(int nx, int ny, int nz, unsigned flags, const tf_tile_config *tile,
+                    tf_tile_config *out);
 
 int tf_abi_version(void);
 const char *tf_status_string(int status);

@@ -109,3 +109,23 @@ def test_python_api_validates_before_launch():
     with pytest.raises(NotImplementedError):
         tg.time_integration.time_integration(torch.zeros(5, 3, 3, 3), 0.1, 0.2, 5 / 3, False,
                                              True)
+
+
+def test_tile_choice(lib):
+    """The built-in tile choice (no GPU needed: dimensions and flags only):
+    the y-marching 8-row tile where it computes no more cells than the
+    x-marching 16-row tile (fast arithmetic, periodic, even nz), else the
+    x-marching tile; explicit tiles are taken as given."""
+    import tinyfluids_gb300 as tg
+    assert tg.resolved_tile((512, 512, 512), exact=False)[::2] == (8, "ym")
+    assert tg.resolved_tile((768, 768, 768), exact=False)[::2] == (8, "ym")
+    assert tg.resolved_tile((128, 128, 128), exact=False)[::2] == (16, "ldg")
+    assert tg.resolved_tile((512, 512, 512), exact=True)[::2] == (16, "ldg")
+    assert tg.resolved_tile((512, 512, 512), True, exact=False)[::2] == (16, "ldg")
+    assert tg.resolved_tile((512, 512, 511), exact=False)[::2] == (16, "ldg")
+    rows, lx, lay = tg.resolved_tile((512, 512, 512), exact=False)
+    assert 16 <= lx <= 64
+    assert tg.resolved_tile((64, 64, 64), exact=False, tile=(8, 5, "ym")) == (8, 5, "ym")
+    assert tg.resolved_tile((64, 64, 64), exact=False, tile=(32, 7)) == (32, 7, "ldg")
+    with pytest.raises(tg.TinyfluidsError):
+        tg.resolved_tile((64, 64, 64), exact=False, tile=(32, 0, "ym"))

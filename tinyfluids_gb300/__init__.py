@@ -12,7 +12,8 @@ from .fluid import (DENSITY_INDEX, PRESSURE_INDEX, VAR_AXIS, VELOCITY_X_INDEX,  
                     _cfl_time_step, _euler_flux, _evolve_state, _evolve_state_along_axis,
                     _hll_solver, _open_boundaries, conserved_state_from_primitive,
                     exact_arithmetic, get_max_wave_speeds, get_wave_speeds,
-                    primitive_state_from_conserved, set_exact, speed_of_sound)
+                    primitive_state_from_conserved, resolved_tile, set_exact,
+                    speed_of_sound)
 from .initial_conditions import overpressure, setup_ics, shear_layer  # noqa: F401
 from .time_integration import run_steps, step  # noqa: F401
 from .time_integration import time_integration as time_integration_fn  # noqa: F401

@@ -59,6 +59,7 @@ SIGNATURES = {
     "tf_evolve_state_diag": (c_int, [vp, vp, c_int, c_int, c_int, c_float, c_float, vp,
                                      c_float, c_uint, vp, vp, vp, c_int, vp]),
     "tf_diagnostics": (c_int, [vp, c_int, c_int, c_int, c_float, vp, vp, c_int, vp]),
+    "tf_resolve_tile": (c_int, [c_int, c_int, c_int, c_uint, vp, vp]),
     "tf_debug_checked": (c_int, []),
     "tf_debug_set_graph_loop_cap": (c_int, [c_int]),
     "tf_debug_reset": (c_int, [vp, c_ll]),

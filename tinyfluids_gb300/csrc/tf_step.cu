@@ -542,10 +542,10 @@ static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int
   return g;
 }
 
-// Fraction of extra cells a layout computes for a grid (ring and ragged
+// Cells a layout computes per stored cell for a grid (ring and ragged
 // tiles): the x-marching 16-row tile stores 30 x 14 of 32 x 16 cells; the
 // y-marching 8-row tile stores 60 of 64 z cells and derives two halo rows per
-// 4 rows (about 7.8% more arithmetic, measured on the FP32 pipe counters).
+// 4 rows (about 7.8% more arithmetic, from the FP32 pipe counters).
 static double overlap_xmarch(int ny, int nz) {
   const double y = (double)((ny + 13) / 14) * 16 / ny;
   const double z = (double)((nz + kTileZ - 1) / kTileZ) * kTileLanes / nz;
@@ -557,12 +557,14 @@ static double overlap_ymarch(int nz) {
 
 // The tile of a fused step.  With no tile given, the fast and diagnostics
 // steps on a periodic grid with an even nz and at least 4 x rows take the
-// y-marching 8-row tile when it computes at least 7% fewer cells than the
-// x-marching 16-row tile (measured on GB300: 86-87 against 83-84
-// Gcell-updates/s for the 512^3 shear layer; within 2% of each other at 384^3
-// and 768^3 and slower below 384^3, where the rule keeps the x-marching tile);
-// otherwise the x-marching 16-row tile (two CTAs per SM interleave their
-// barrier phases).  loader 3 selects the y-marching tile explicitly.
+// y-marching 8-row tile when it computes no more cells than the x-marching
+// 16-row tile, else the x-marching 16-row tile (two CTAs per SM interleave
+// their barrier phases).  Measured on GB300 (shear layer, Gcell-updates/s,
+// x-marching / y-marching): 128^3 46.4 / 42.3, 192^3 66.2 / 63.7, 256^3
+// 72.8 / 73.7, 320^3 80.5 / 80.2, 384^3 81.6 / 84.6, 448^3 87.6 / 87.0,
+// 512^3 83.7 / 89.3, 640^3 86.7 / 89.9, 768^3 87.6 / 91.9, 1024^3 84.9 /
+// 85.6; the rule picks the faster one except at the near-ties 256^3 and
+// 320^3.  loader 3 selects the y-marching tile explicitly.
 static int resolve_tile(const tf_tile_config* tile, int nx, int ny, int nz, unsigned flags,
                         int* rows, int* lx, int* loader) {
   *rows = 16;
@@ -584,7 +586,7 @@ static int resolve_tile(const tf_tile_config* tile, int nx, int ny, int nz, unsi
   }
   const bool fit = !(flags & (TF_FLAG_EXACT | TF_FLAG_OPEN_BOUNDARIES)) && (nz & 1) == 0 &&
                    nx >= 4;
-  if (fit && overlap_xmarch(ny, nz) >= 1.07 * overlap_ymarch(nz)) {
+  if (fit && overlap_xmarch(ny, nz) >= overlap_ymarch(nz)) {
     *rows = 8;
     *loader = 3;
   }
@@ -1123,6 +1125,19 @@ int tf_evolve_state_diag(const float* W_in, float* W_out, int nx, int ny, int nz
   cudaStream_t s = (cudaStream_t)stream;
   TF_TRY(cuda_check(cudaMemsetAsync(totals, 0, 5 * sizeof(double), s), "cudaMemsetAsync"));
   return launch_fused(a, rows, (flags & TF_FLAG_EXACT) != 0, s, 1);
+}
+
+int tf_resolve_tile(int nx, int ny, int nz, unsigned flags, const tf_tile_config* tile,
+                    tf_tile_config* out) {
+  if (!out) return set_error(TF_ERR_ARG, "null output");
+  TF_TRY(check_dims(nx, ny, nz, flags));
+  int rows, lx, loader;
+  TF_TRY(resolve_tile(tile, nx, ny, nz, flags, &rows, &lx, &loader));
+  const FusedGeom g = make_geom(nx, ny, nz, flags, rows, lx, loader == 3 ? 1 : 0);
+  out->rows = rows;
+  out->lx = g.lx;
+  out->loader = loader;
+  return TF_OK;
 }
 
 int tf_debug_checked(void) { return TF_CHECKED; }

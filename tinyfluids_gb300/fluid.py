@@ -309,6 +309,17 @@ def _evolve_state_along_axis(primitive_state, grid_spacing, dt, gamma, axis, *,
     return out
 
 
+def resolved_tile(shape, handle_boundaries=False, exact=None, tile=None):
+    """The tile a fused step on a grid of `shape` (nx, ny, nz) runs:
+    (rows, lx, layout) with layout "ldg" / "tma" (x-marching) or "ym"
+    (y-marching) and the chunk length resolved."""
+    nx, ny, nz = (int(v) for v in shape)
+    out = _lib.TileConfig()
+    _lib.call("tf_resolve_tile", nx, ny, nz, _flags(handle_boundaries, exact),
+              _tile_arg(tile, None, exact), ctypes.byref(out))
+    return out.rows, out.lx, {0: "ldg", 1: "ldg", 2: "tma", 3: "ym"}[out.loader]
+
+
 def _tile_arg(tile, state=None, exact=None):
     """tf_tile_config for `tile`: None (built-in choice), (rows, lx),
     (rows, lx, loader) with loader "auto" | "ldg" | "tma" (x-marching tile)
