@@ -252,7 +252,7 @@ int tf_sweep_conserved_f64(const double *U, double *out, int nx, int ny, int nz,
  * loads it, held until exit), so the caller passes only W_in and W_out, and
  * nothing is allocated.  Grids above TF_NOALLOC_MAX_CELLS cells are rejected
  * with TF_ERR_ARG, and so are states whose bytes overlap each other or the
- * scratch.  The run uses tf_time_integration's default tile (16 rows).  The
+ * scratch.  The run uses tf_time_integration's built-in tile choice.  The
  * first call on a device looks up the scratch's device address and caches it
  * for the life of the process; make that first call before any stream
  * capture, and do not use the entry point across a cudaDeviceReset (which
