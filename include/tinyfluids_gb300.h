@@ -155,6 +155,11 @@ int tf_debug_checked(void);
  * on (cap <= 0 or above the default restores the default 2^24): lets a test
  * run a loop into its bound. */
 int tf_debug_set_graph_loop_cap(int cap);
+/* The simulated time tf_time_integration loops start from (default 0, the
+ * reference's, time_integration.py:66; t0 must be finite and >= 0): lets a
+ * test start a loop where float32 t no longer advances by dt and see the
+ * stall reported.  No reference counterpart (a test hook). */
+int tf_debug_set_loop_start_time(float t0);
 int tf_debug_reset(int *write_counts, long long ncells);
 long long tf_debug_oob_count(void);
 /* The adjoint sweep of tf_adjoint_sweep computed one thread per cell with

@@ -6,6 +6,7 @@ FAST_STEP_RTOL per step (relative to each variable's max magnitude) and its
 density error against the FP64 oracle stays within 2x the reference float32
 scheme's own error.
 """
+import ctypes
 import json
 import os
 
@@ -324,6 +325,25 @@ def test_graph_loop_stops_at_its_evaluation_cap(tg):
     finally:
         lib.tf_debug_set_graph_loop_cap(0)
     _, it = tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False)
+    assert int(it) == GOLDEN["counts"]["32"]
+
+
+@pytest.mark.parametrize("host_loop", [False, True])
+def test_stalled_time_is_reported(tg, host_loop):
+    """A loop whose float32 t no longer advances (t + dt == t: the reference
+    would loop forever) stops with TF_ERR_NONFINITE, in the device-side graph
+    loop and in the host-checked loop; the loop starts at t = 1e7 through the
+    test hook, where the ~1e-3 CFL steps of this state round away."""
+    W, dx = tg.setup_ics(32, 2)
+    lib = tg._lib.load()
+    assert lib.tf_debug_set_loop_start_time(ctypes.c_float(1e7)) == 0
+    try:
+        with pytest.raises(tg.TinyfluidsError) as e:
+            tg.time_integration_fn(W, dx, 2e7, GAMMA, True, False, host_loop=host_loop)
+        assert e.value.status == 3, str(e.value)
+    finally:
+        assert lib.tf_debug_set_loop_start_time(ctypes.c_float(0.0)) == 0
+    _, it = tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False, host_loop=host_loop)
     assert int(it) == GOLDEN["counts"]["32"]
 
 

@@ -127,8 +127,9 @@ static int elementwise_grid(long long n) {
 // ---------------------------------------------------------------------------
 // control block
 // ---------------------------------------------------------------------------
-__global__ void ctl_init_kernel(tf_ctl* ctl, float t_final, float cfl_dx, int max_steps) {
-  ctl->t = 0.f;
+__global__ void ctl_init_kernel(tf_ctl* ctl, float t_final, float cfl_dx, int max_steps,
+                                float t0 = 0.f) {
+  ctl->t = t0;
   ctl->dt = 0.f;
   ctl->t_final = t_final;
   ctl->cfl_dx = cfl_dx;
@@ -153,6 +154,10 @@ constexpr int kGraphLoopCap = 1 << 24;
 // the cap new loop graphs get (tf_debug_set_graph_loop_cap lowers it so a
 // test can run into it)
 static std::atomic<int> g_graph_loop_cap{kGraphLoopCap};
+// the time a tf_time_integration loop starts from: 0 as in the reference
+// (time_integration.py:66); tf_debug_set_loop_start_time changes it so a
+// test can drive a loop into its float32 stall guard
+static std::atomic<float> g_loop_t0{0.f};
 
 __global__ void loop_cond_kernel(tf_ctl* ctl, cudaGraphConditionalHandle h, int cap) {
   const int evals = ctl->reserved[0] + 1;
@@ -1147,6 +1152,12 @@ int tf_debug_set_graph_loop_cap(int cap) {
   return TF_OK;
 }
 
+int tf_debug_set_loop_start_time(float t0) {
+  if (!isfinite(t0) || t0 < 0.f) return set_error(TF_ERR_ARG, "start time must be finite and >= 0");
+  g_loop_t0.store(t0);
+  return TF_OK;
+}
+
 int tf_debug_reset(int* write_counts, long long ncells) {
 #if TF_CHECKED
   unsigned long long zero = 0;
@@ -1212,7 +1223,7 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
   const long long n = (long long)nx * ny * nz;
   const bool exact = (flags & TF_FLAG_EXACT) != 0;
 
-  ctl_init_kernel<<<1, 1, 0, s>>>(ctl, t_final, cfl * dx, max_steps);
+  ctl_init_kernel<<<1, 1, 0, s>>>(ctl, t_final, cfl * dx, max_steps, g_loop_t0.load());
   maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W_in, n, gamma, ctl, exact ? 0 : 1);
   TF_TRY(launch_check("maxspeed_kernel"));
 
