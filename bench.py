@@ -47,7 +47,8 @@ def parse():
     p.add_argument("--e2e-repeats", type=int, default=4)
     p.add_argument("--cpu-sample-seconds", type=float, default=20.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--tile", default=None, help="rows,lx of the fused kernel")
+    p.add_argument("--tile", default=None,
+                   help="rows,lx[,layout] of the fused kernel (layout: ldg, tma or ym)")
     p.add_argument("--out", default=None, help="also write the JSON line here")
     p.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "adjoint"],
                    help="plain: 512^3 step (default); batch: 256 uneven instances in one "
@@ -59,6 +60,10 @@ def parse():
     p.add_argument("--serve-rate", type=float, default=200.0,
                    help="arrival rate of the serving part of the default line")
     p.add_argument("--serve-requests", type=int, default=300)
+    p.add_argument("--serve-rate-light", type=float, default=40.0,
+                   help="a second arrival rate of the default line, below the GPU's "
+                        "capacity for this request mix (about 60 solves/s), where "
+                        "latencies are not dominated by the backlog")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the serving and batching parts of the default line")
     return p.parse_args()
@@ -357,6 +362,8 @@ def run_gpu(args):
         del W, out, ctl, Wh, Oh
         torch.cuda.empty_cache()
         line["serving"] = measure_serving(torch, tg, dev, args.serve_rate, args.serve_requests)
+        line["serving_light_load"] = measure_serving(torch, tg, dev, args.serve_rate_light,
+                                                     args.serve_requests)
         line["batching"] = measure_batching(torch, tg, dev, 256, 100, 3)
     emit(line, args.out)
     return 0
