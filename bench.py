@@ -330,8 +330,8 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": max(3, Wu), "ms_per_step": ms / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"shear layer {n}^3, gamma=5/3, CFL 0.4, periodic, "
-                               f"{K} steps per run",
+        "config": {"workload": f"shear layer {n}^3, gamma=5/3, CFL 0.4, periodic",
+                   "steps_per_run": K,
                    "instances": world,
                    "parallelism": "replicas" if world > 1 else "single",
                    "arithmetic": "exact" if args.exact else "fast",
