@@ -160,6 +160,10 @@ int tf_debug_set_graph_loop_cap(int cap);
  * test start a loop where float32 t no longer advances by dt and see the
  * stall reported.  No reference counterpart (a test hook). */
 int tf_debug_set_loop_start_time(float t0);
+/* on != 0: fused steps use the 64-bit addressing form that grids of 2^31 or
+ * more cells take (both tiles), on every grid, so a test can check that form
+ * on small grids; 0 restores the default.  No reference counterpart. */
+int tf_debug_force_64bit_offsets(int on);
 int tf_debug_reset(int *write_counts, long long ncells);
 long long tf_debug_oob_count(void);
 /* The adjoint sweep of tf_adjoint_sweep computed one thread per cell with

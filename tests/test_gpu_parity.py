@@ -347,6 +347,28 @@ def test_stalled_time_is_reported(tg, host_loop):
     assert int(it) == GOLDEN["counts"]["32"]
 
 
+@pytest.mark.parametrize("shape", [(40, 31, 64), (13, 9, 121), (9, 13, 62)])
+def test_64bit_addressing_form_bitwise(tg, shape):
+    """The addressing form of grids of 2^31 or more cells (64-bit offsets),
+    forced on small grids through the test hook, gives the same bits as the
+    32-bit form in both tiles, fast and conserved."""
+    W = dev(random_state(shape, 71))
+    U = tg.conserved_state_from_primitive(W, GAMMA)
+    tiles = (None, (16, 0, "ldg"), (8, 0, "ym"), (16, 3, "ym"))
+    ref = [tg._evolve_state(W, 0.05, 2e-3, GAMMA, tile=t) for t in tiles]
+    refc = tg._evolve_state(U, 0.05, 2e-3, GAMMA, conserved=True)
+    lib = tg._lib.load()
+    assert lib.tf_debug_force_64bit_offsets(1) == 0
+    try:
+        out = [tg._evolve_state(W, 0.05, 2e-3, GAMMA, tile=t) for t in tiles]
+        outc = tg._evolve_state(U, 0.05, 2e-3, GAMMA, conserved=True)
+    finally:
+        assert lib.tf_debug_force_64bit_offsets(0) == 0
+    for t, a, b in zip(tiles, ref, out):
+        assert torch.equal(a, b), t
+    assert torch.equal(refc, outc)
+
+
 def test_empty_axis_rejected(tg):
     with pytest.raises(ValueError):
         tg._evolve_state(torch.zeros(5, 0, 4, 4, device="cuda"), 0.1, 1e-3, GAMMA)

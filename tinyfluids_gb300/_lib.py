@@ -63,6 +63,7 @@ SIGNATURES = {
     "tf_debug_checked": (c_int, []),
     "tf_debug_set_graph_loop_cap": (c_int, [c_int]),
     "tf_debug_set_loop_start_time": (c_int, [c_float]),
+    "tf_debug_force_64bit_offsets": (c_int, [c_int]),
     "tf_debug_reset": (c_int, [vp, c_ll]),
     "tf_debug_oob_count": (c_ll, []),
     "tf_debug_adjoint_sweep_per_cell": (c_int, [vp, vp, vp, c_int, c_int, c_int, c_float,

@@ -158,6 +158,10 @@ static std::atomic<int> g_graph_loop_cap{kGraphLoopCap};
 // (time_integration.py:66); tf_debug_set_loop_start_time changes it so a
 // test can drive a loop into its float32 stall guard
 static std::atomic<float> g_loop_t0{0.f};
+// the fused steps of grids under 2^31 cells address with 32-bit offsets from
+// per-variable bases; tf_debug_force_64bit_offsets makes them take the 64-bit
+// form that larger grids use, so a test can check it on small grids
+static std::atomic<bool> g_force_64bit{false};
 
 __global__ void loop_cond_kernel(tf_ctl* ctl, cudaGraphConditionalHandle h, int cap) {
   const int evals = ctl->reserved[0] + 1;
@@ -658,7 +662,7 @@ static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_
     a.geo.pairs8 = ((reinterpret_cast<uintptr_t>(a.src) | reinterpret_cast<uintptr_t>(a.dst)) &
                     7) == 0 && (vs & 1) == 0 && (a.geo.nz & 1) == 0;
     const dim3 g(a.geo.tiles_x, a.geo.tiles_z, a.geo.tiles_y);
-    const bool vp = vs < (1ull << 31);
+    const bool vp = vs < (1ull << 31) && !g_force_64bit.load();
     // 8-byte pair accesses: periodic wrap keeps every pair whole when nz is even
     const bool vec = a.geo.pairs8 && !a.geo.open_bc;
     int st = TF_OK;
@@ -684,6 +688,8 @@ static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_
         launch(YmTag<FastPair, NW, false, true, true>{});
       } else if (vp) {
         launch(YmTag<FastPair, NW, false, true>{});
+      } else if (vec) {
+        launch(YmTag<FastPair, NW, false, false, true>{});
       } else {
         launch(YmTag<FastPair, NW, false, false>{});
       }
@@ -713,17 +719,13 @@ static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_
     if (exact || rows != 16)
       return set_error(TF_ERR_UNSUPPORTED,
                        "conserved input/output: fast arithmetic and 16-row tiles only");
-    if (vs < (1ull << 31))
+    if (vs < (1ull << 31) && !g_force_64bit.load())
       fused_step_kernel<FastPairConserved, 8, false, true><<<grid, 8 * 32, 0, s>>>(a);
     else
       fused_step_kernel<FastPairConserved, 8><<<grid, 8 * 32, 0, s>>>(a);
     return launch_check("fused_step_kernel (conserved)");
   }
-#ifndef TF_NO_VP
-  const bool vp32 = vs < (1ull << 31);
-#else
-  const bool vp32 = false;
-#endif
+  const bool vp32 = vs < (1ull << 31) && !g_force_64bit.load();
   TF_DISPATCH_ROWS(rows, NWP, {
     if (exact) fused_step_kernel<ExactPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
     else if (vp32) fused_step_kernel<FastPair, NWP, false, true><<<grid, NWP * 32, 0, s>>>(a);
@@ -1149,6 +1151,11 @@ int tf_debug_checked(void) { return TF_CHECKED; }
 
 int tf_debug_set_graph_loop_cap(int cap) {
   g_graph_loop_cap.store(cap > 0 && cap < kGraphLoopCap ? cap : kGraphLoopCap);
+  return TF_OK;
+}
+
+int tf_debug_force_64bit_offsets(int on) {
+  g_force_64bit.store(on != 0);
   return TF_OK;
 }
 
