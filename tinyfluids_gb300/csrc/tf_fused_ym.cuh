@@ -3,11 +3,12 @@
 // (tf_fused.cuh), with the axes given other roles so that fewer cells are
 // computed twice.
 //
-// Decomposition.  A CTA owns NW consecutive x rows (one per warp) of 62 z
+// Decomposition.  A CTA owns NW consecutive x rows (one per warp) of 60 z
 // cells and MARCHES along y through a chunk of planes.  Lane l of a warp owns
-// the PAIR of z-adjacent cells z0-1+2l and z0+2l (packed f32x2 arithmetic,
-// tf_pair.cuh), so a warp spans 64 cells of z: lane 0's first and lane 31's
-// second cell are a one-cell ring that is swept but not stored.
+// the PAIR of z-adjacent cells 60*tz-2+2l and 60*tz-1+2l (packed f32x2
+// arithmetic, tf_pair.cuh), so a warp spans 64 cells of z: lanes 0 and 31
+// hold the ring (swept, not stored) and a pair starts at an even z, so it
+// moves as one 8-byte access when the grid allows.
 //
 //  * x sweep (the first sweep) across the warps: every warp derives its own
 //    row, writes it to shared memory, and solves the face above its row from
@@ -27,8 +28,8 @@
 //
 // Compared with the x-marching tile (32 lanes x 2 rows per warp, 30 x 14
 // cells stored of 32 x 16 computed) the only recomputed cells are the z ring
-// (62 of 64) and the two derived halo rows per CTA, and the z exchange
-// shuffles half as many values.  Every load index is wrapped periodically
+// (60 stored of 64) and the two derived halo rows per CTA, the z exchange
+// shuffles half as many values and the global accesses move 8-byte pairs.  Every load index is wrapped periodically
 // in-kernel (and clamped for open boundaries), so any nx, ny, nz >= 1 works.
 // Results equal the x-marching tile's bit for bit: each face and each update
 // is the same operation sequence on the same operands.
@@ -38,7 +39,6 @@
 #include "tf_fused.cuh"
 
 namespace tf {
-
 
 constexpr int kYmZ = 60;  // stored z cells per tile: lanes 1..30 (lanes 0 and 31 are the ring)
 
@@ -107,8 +107,8 @@ __device__ __forceinline__ void ym_get_face(const YmSmem<NW>& sm, int s, int l, 
   f[4] = sm.fx4[s][l];
 }
 
-// Per-lane asynchronous 4- and 8-byte copies global -> shared (cached in L1), and their
-// group bookkeeping (PTX ISA: cp.async, cp.async.commit_group,
+// Per-lane asynchronous 4- and 8-byte copies global -> shared (cached in
+// L1) and their group bookkeeping (PTX ISA: cp.async, cp.async.commit_group,
 // cp.async.wait_group).
 __device__ __forceinline__ void cp_async4(void* smem, const float* gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(smem)), "l"(gmem)
