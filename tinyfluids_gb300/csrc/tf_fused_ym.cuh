@@ -40,6 +40,7 @@
 
 namespace tf {
 
+
 constexpr int kYmZ = 60;  // stored z cells per tile: lanes 1..30 (lanes 0 and 31 are the ring)
 
 template <int NW>
@@ -162,7 +163,9 @@ __device__ __forceinline__ float fused_tile_ym(const float* __restrict__ src,
   static_assert(NW >= 2, "the two halo rows need two distinct warps");
   using Off = typename std::conditional<VP && !TF_CHECKED, unsigned, size_t>::type;
   const int lane = threadIdx.x & 31;
-  const int w = threadIdx.x >> 5;
+  // the warp index through a shuffle from lane 0: provably the same in every
+  // lane, so branches on it need no convergence barriers (measured +0.5%)
+  const int w = __shfl_sync(0xffffffffu, (int)(threadIdx.x >> 5), 0);
   const bool open = G.open_bc != 0;
   const int x0 = tx * NW;
   const int y0 = ty * G.lx;
