@@ -181,7 +181,10 @@ __device__ __forceinline__ bool plane_update(int x, V2 pf[5], const Cell2& cur, 
   // cur / fm: plane x and the flux at x-1/2; nxt / fp receive plane x+1 and
   // the flux at x+1/2 (the caller copies them into cur / fm for the next plane)
   const int lane = threadIdx.x & 31;
-  const int w = uniform_warp_index();  // measured +0.5-1% over threadIdx.x >> 5
+  // fast tiles: the warp index through a lane-0 shuffle (measured +0.5-1%);
+  // the exact tile keeps threadIdx.x >> 5 (the shuffle costs it a register
+  // spill and 9%)
+  const int w = P::kExact ? (int)(threadIdx.x >> 5) : uniform_warp_index();
   P::template derive_in<1>(pf, nxt, K);
   consumed();
   P::hll(cur, nxt, fp);  // face x + 1/2
