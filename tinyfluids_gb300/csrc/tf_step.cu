@@ -521,17 +521,21 @@ static FusedGeom make_geom(int nx, int ny, int nz, unsigned flags, int rows, int
   g.tiles_z = (nz + kTileZ - 1) / kTileZ;
   g.tiles_y = (ny + (rows - 2) - 1) / (rows - 2);
   if (lx <= 0) {
-    // About 9 waves of resident CTAs, in chunks of >= 16 planes (each chunk
-    // re-reads one plane and warms up its carry); grids too small for one
-    // wave at that chunk length take 8-plane chunks, and grids too small for
-    // one wave even then are latency-bound and take the chunk length that
-    // makes one wave, but at least 2 planes.  Measured on GB300 with the
-    // reference's benchmark states: 32^3 -> 2 planes, 64^3 -> 4, 96^3 -> 8,
-    // 128^3 and 256^3 -> 16, 512^3 -> 103 (5 chunks).
+    // About 9 waves of resident CTAs, in chunks of >= 32 planes where those
+    // still make 1.5 waves, else >= 16 planes (each chunk re-reads one plane
+    // and warms up its carry); grids too small for one wave at 16 planes take
+    // 8-plane chunks, and grids too small for one wave even then are
+    // latency-bound and take the chunk length that makes one wave, but at
+    // least 2 planes.  Measured on GB300 (shear layer, 16-row tiles, chunk
+    // length: Gcell-updates/s): 160^3 16: 58.5, 32: 50.6; 192^3 16: 66.2, 32:
+    // 68.6; 256^3 16: 73.0, 32: 75.6; the reference's benchmark states: 32^3
+    // -> 2 planes, 64^3 -> 4, 96^3 -> 8, 128^3 -> 16, 512^3 -> 103.
     const long long tiles_yz = (long long)g.tiles_z * g.tiles_y;
     const long long resident = (long long)sm_count() * min_ctas_per_sm(rows / 2);
     long long min_planes;
-    if (tiles_yz * (nx / 16) >= resident) {
+    if (2 * tiles_yz * (nx / 32) >= 3 * resident) {
+      min_planes = 32;
+    } else if (tiles_yz * (nx / 16) >= resident) {
       min_planes = 16;
     } else if (tiles_yz * (nx / 8) >= resident) {
       min_planes = 8;
@@ -567,8 +571,8 @@ static double overlap_ymarch(int nz) {
 // The tile of a fused step.  With no tile given, the fast and diagnostics
 // steps on a periodic grid with an even nz and at least 4 x rows take the
 // y-marching 8-row tile when it computes no more cells than the x-marching
-// 16-row tile, else the x-marching 16-row tile (two CTAs per SM interleave
-// their barrier phases).  Measured on GB300 (shear layer, Gcell-updates/s,
+// 16-row tile, else the x-marching tile: 8 rows for grids of at most 128^3
+// cells, 16 rows above (two CTAs per SM interleave their barrier phases).  Measured on GB300 (shear layer, Gcell-updates/s,
 // x-marching / y-marching): 128^3 46.4 / 42.3, 192^3 66.2 / 63.7, 256^3
 // 72.8 / 73.7, 320^3 80.5 / 80.2, 384^3 81.6 / 84.6, 448^3 87.6 / 87.0,
 // 512^3 83.7 / 89.3, 640^3 86.7 / 89.9, 768^3 87.6 / 91.9, 1024^3 84.9 /
@@ -598,6 +602,13 @@ static int resolve_tile(const tf_tile_config* tile, int nx, int ny, int nz, unsi
   if (fit && overlap_xmarch(ny, nz) >= overlap_ymarch(nz)) {
     *rows = 8;
     *loader = 3;
+  } else if ((long long)nx * ny * nz <= (1LL << 21) &&
+             !(flags & (TF_FLAG_IN_CONSERVED | TF_FLAG_OUT_CONSERVED))) {
+    // grids of at most 128^3 cells: 8-row x-marching tiles (four CTAs per SM
+    // fill the GPU better; measured 96^3 34.6 vs 34.0, 128^3 49.0 vs 47.4
+    // Gcell-updates/s against 16 rows, equal below); the conserved-state step
+    // keeps its 16-row tile
+    *rows = 8;
   }
   return TF_OK;
 }
