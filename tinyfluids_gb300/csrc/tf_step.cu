@@ -163,7 +163,24 @@ static std::atomic<float> g_loop_t0{0.f};
 // form that larger grids use, so a test can check it on small grids
 static std::atomic<bool> g_force_64bit{false};
 
+#ifndef TF_PDL
+#define TF_PDL 1
+#endif
+// Programmatic dependent launch: a step kernel waits for the grid before it
+// in the stream to complete (and its writes to be visible) before it reads
+// anything, then lets the next step's grid launch as soon as every one of its
+// own CTAs has started, so the next launch's latency and CTA setup overlap
+// this grid's last wave (6-16% per step on 32^3-128^3 grids, under 1% from
+// 256^3 up).  Build with -DTF_PDL=0 for plain stream-ordered launches.
+__device__ __forceinline__ void pdl_wait_and_release() {
+#if TF_PDL
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
 __global__ void loop_cond_kernel(tf_ctl* ctl, cudaGraphConditionalHandle h, int cap) {
+  pdl_wait_and_release();
   const int evals = ctl->reserved[0] + 1;
   const float t = ld_volatile(&ctl->t);
   const float t_prev = __int_as_float(ctl->reserved[1]);
@@ -356,6 +373,7 @@ template <class P, int NWP, bool DIAG = false, bool VP = false>
 __global__ void TF_FUSED_BOUNDS(NWP) fused_step_kernel(const __grid_constant__ FusedArgs a) {
   __shared__ FusedSmem<NWP> sm;
   __shared__ double dred[DIAG ? NWP * 5 : 1];
+  pdl_wait_and_release();
   float dt;
   if (!launch_dt(a, &dt)) return;
   const StepConsts<float> K = launch_consts(a, dt);
@@ -378,6 +396,7 @@ __global__ void __launch_bounds__(NW * 32, min_ctas_per_sm(NW))
   extern __shared__ __align__(16) unsigned char ym_smem[];
   YmSmem<NW>& sm = *reinterpret_cast<YmSmem<NW>*>(ym_smem);
   __shared__ double dred[DIAG ? NW * 5 : 1];
+  pdl_wait_and_release();
   float dt;
   if (!launch_dt(a, &dt)) return;
   const StepConsts<float> K = launch_consts(a, dt);
@@ -625,6 +644,29 @@ static int launch_tma(const FusedArgs& a, dim3 grid, const CUtensorMap& tm, bool
   return TF_OK;
 }
 
+// Launches a step (or loop condition) kernel; with TF_PDL, as a programmatic
+// dependent of the work before it in the stream (the kernel waits for that
+// work itself).
+template <class... KArgs, class... Args>
+static void launch_step(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                        cudaStream_t s, Args... args) {
+#if TF_PDL
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, args...);
+#else
+  kern<<<grid, block, smem, s>>>(args...);
+#endif
+}
+
 // Template arguments of one y-marching kernel instantiation.
 template <class P_, int NW_, bool DIAG_, bool VP_, bool VEC_ = false>
 struct YmTag {
@@ -684,7 +726,7 @@ static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_
         auto kern = fused_step_ym_kernel<typename T::P, NW, T::diag, T::vp, T::vec>;
         const size_t smem = ym_smem_bytes(NW);
         st = ym_smem_attr<T>(kern, smem);
-        if (st == TF_OK) kern<<<g, NW * 32, smem, s>>>(a);
+        if (st == TF_OK) launch_step(kern, g, dim3(NW * 32), smem, s, a);
       };
       if (a.totals) {
         if (exact) launch(YmTag<ExactPair, NW, true, false>{});
@@ -721,8 +763,8 @@ static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_
   }
   if (a.totals) {
     TF_DISPATCH_ROWS(rows, NWP, {
-      if (exact) fused_step_kernel<ExactPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
-      else fused_step_kernel<FastPair, NWP, true><<<grid, NWP * 32, 0, s>>>(a);
+      if (exact) launch_step(fused_step_kernel<ExactPair, NWP, true>, grid, dim3(NWP * 32), 0, s, a);
+      else launch_step(fused_step_kernel<FastPair, NWP, true>, grid, dim3(NWP * 32), 0, s, a);
     });
     return launch_check("fused_step_kernel (diagnostics)");
   }
@@ -731,16 +773,17 @@ static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_
       return set_error(TF_ERR_UNSUPPORTED,
                        "conserved input/output: fast arithmetic and 16-row tiles only");
     if (vs < (1ull << 31) && !g_force_64bit.load())
-      fused_step_kernel<FastPairConserved, 8, false, true><<<grid, 8 * 32, 0, s>>>(a);
+      launch_step(fused_step_kernel<FastPairConserved, 8, false, true>, grid, dim3(8 * 32), 0, s, a);
     else
-      fused_step_kernel<FastPairConserved, 8><<<grid, 8 * 32, 0, s>>>(a);
+      launch_step(fused_step_kernel<FastPairConserved, 8>, grid, dim3(8 * 32), 0, s, a);
     return launch_check("fused_step_kernel (conserved)");
   }
   const bool vp32 = vs < (1ull << 31) && !g_force_64bit.load();
   TF_DISPATCH_ROWS(rows, NWP, {
-    if (exact) fused_step_kernel<ExactPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
-    else if (vp32) fused_step_kernel<FastPair, NWP, false, true><<<grid, NWP * 32, 0, s>>>(a);
-    else fused_step_kernel<FastPair, NWP><<<grid, NWP * 32, 0, s>>>(a);
+    if (exact) launch_step(fused_step_kernel<ExactPair, NWP>, grid, dim3(NWP * 32), 0, s, a);
+    else if (vp32)
+      launch_step(fused_step_kernel<FastPair, NWP, false, true>, grid, dim3(NWP * 32), 0, s, a);
+    else launch_step(fused_step_kernel<FastPair, NWP>, grid, dim3(NWP * 32), 0, s, a);
   });
   return launch_check("fused_step_kernel");
 }
@@ -850,11 +893,11 @@ static int build_graph_loop(const FusedArgs& a, const LoopBufs& b, int rows, boo
              "cudaStreamBeginCaptureToGraph"))
       break;
     capturing = true;
-    loop_cond_kernel<<<1, 1, 0, cs>>>(ctl, h, cap);
+    launch_step(loop_cond_kernel, dim3(1), dim3(1), 0, cs, ctl, h, cap);
     int lst = launch_check("loop_cond_kernel");
     if (lst == TF_OK) lst = launch_fused(step_args(a, b, 1), rows, exact, cs, 1);
     if (lst == TF_OK) {
-      loop_cond_kernel<<<1, 1, 0, cs>>>(ctl, h, cap);
+      launch_step(loop_cond_kernel, dim3(1), dim3(1), 0, cs, ctl, h, cap);
       lst = launch_check("loop_cond_kernel");
     }
     if (lst != TF_OK) {
@@ -891,7 +934,7 @@ static int build_graph_loop(const FusedArgs& a, const LoopBufs& b, int rows, boo
     for (int i = 2; i <= 3 && lst == TF_OK; ++i) {
       lst = launch_fused(step_args(a, b, i), rows, exact, cs, 1);
       if (lst == TF_OK) {
-        loop_cond_kernel<<<1, 1, 0, cs>>>(ctl, h, cap);
+        launch_step(loop_cond_kernel, dim3(1), dim3(1), 0, cs, ctl, h, cap);
         lst = launch_check("loop_cond_kernel");
       }
     }
