@@ -74,8 +74,9 @@ typedef struct tf_ctl {
 
 /* Tile of the fused step kernel; NULL = built-in choice: the y-marching
  * 8-row tile for a fast (or diagnostics / conserved) step on a periodic grid
- * with an even nz where it computes no more cells than the x-marching tile,
- * else the x-marching 16-row tile; the chunk length (lx) for about nine waves
+ * with an even nz and at least 2^17 cells where it computes no more cells
+ * than the x-marching tile, else the x-marching tile (8 rows up to 2^21
+ * cells, 16 above; always 16 for conserved input or output); the chunk length (lx) for about nine waves
  * of resident CTAs in chunks of >= 16 planes (y-marching: <= 64), shorter
  * chunks for grids that would not fill one wave.  tf_resolve_tile reports the
  * choice. */
@@ -151,8 +152,8 @@ int tf_diagnostics(const float *W, int nx, int ny, int nz, float gamma, double *
  * device memory, cell = (x*ny + y)*nz + z) for every cell it stores.  No
  * reference counterpart (the reference has no race or bounds checking). */
 int tf_debug_checked(void);
-/* Evaluation cap of the device-side t_final loop for graphs built from now
- * on (cap <= 0 or above the default restores the default 2^24): lets a test
+/* Step cap of the device-side t_final loop for loops started from now on
+ * (cap <= 0 or above the default restores the default 2^24): lets a test
  * run a loop into its bound. */
 int tf_debug_set_graph_loop_cap(int cap);
 /* The simulated time tf_time_integration loops start from (default 0, the
@@ -183,9 +184,9 @@ int tf_debug_adjoint_sweep_per_cell(const float *U, const float *lam_out, float 
  * blocks until the loop ends and stores the iteration count there.
  * A known step count (max_steps >= 0) enqueues that many predicated steps.
  * A t_final loop (max_steps < 0) runs as one CUDA graph whose while node
- * repeats {step, condition} on the device until the loop condition fails, a
- * step no longer advances float32 t (TF_ERR_NONFINITE: the reference would
- * loop forever) or 2^24 conditions have been evaluated (TF_ERR_TIMEOUT):
+ * repeats {steps, condition} on the device until the loop condition fails,
+ * float32 t no longer advances (TF_ERR_NONFINITE: the reference would loop
+ * forever) or 2^24 steps have run short of t_final (TF_ERR_TIMEOUT):
  * nothing waits on the host.  TF_FLAG_HOST_LOOP instead tests the condition
  * on the host once per chunk of steps. */
 int tf_time_integration(const float *W_in, float *W_out, float *work, tf_ctl *ctl, int nx,

@@ -312,20 +312,23 @@ def test_nonfinite_state_is_reported(tg, host_loop):
     assert e.value.status == 3
 
 
-def test_graph_loop_stops_at_its_evaluation_cap(tg):
-    """The device-side while loop ends after `cap` condition evaluations even
-    though t_final is not reached: TF_ERR_TIMEOUT, exactly cap steps."""
-    W, dx = tg.setup_ics(32, 2)
+@pytest.mark.parametrize("n,cap", [(32, 5), (32, 10), (32, 17), (168, 5)])
+def test_graph_loop_stops_at_its_step_cap(tg, n, cap):
+    """The device-side while loop ends after `cap` steps even though t_final
+    is not reached: TF_ERR_TIMEOUT, exactly cap steps, wherever the cap falls
+    in a while-node body (8 steps per body at 32^3, 2 at 168^3)."""
+    W, dx = tg.setup_ics(n, 2)
     lib = tg._lib.load()
-    lib.tf_debug_set_graph_loop_cap(5)
+    lib.tf_debug_set_graph_loop_cap(cap)
     try:
         with pytest.raises(tg.TinyfluidsError) as e:
             tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False)
-        assert e.value.status == 4 and "after 5 steps" in str(e.value)
+        assert e.value.status == 4 and ("after %d steps" % cap) in str(e.value)
     finally:
         lib.tf_debug_set_graph_loop_cap(0)
-    _, it = tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False)
-    assert int(it) == GOLDEN["counts"]["32"]
+    if n == 32:
+        _, it = tg.time_integration_fn(W, dx, 0.2, GAMMA, True, False)
+        assert int(it) == GOLDEN["counts"]["32"]
 
 
 @pytest.mark.parametrize("host_loop", [False, True])

@@ -146,13 +146,16 @@ __global__ void ctl_init_kernel(tf_ctl* ctl, float t_final, float cfl_dx, int ma
 // Condition of the device-side t_final loop (a CUDA graph while node): the
 // loop condition the last step left in ctl->active, stopped early when
 // float32 t did not advance since the previous evaluation (a stalled loop
-// the reference would never leave) or after `cap` evaluations.  Every body
-// iteration runs this kernel once, so the evaluation count bounds the loop
-// whatever the step kernel does.  ctl->reserved[0] counts evaluations,
-// reserved[1] holds the bits of t at the previous one.
+// the reference would never leave) or after `cap` steps.  The loop's
+// control block carries max_steps = cap, so the step kernels themselves stop
+// after exactly `cap` steps; a loop that stopped there short of t_final is
+// reported as TF_ERR_TIMEOUT.  Every body iteration runs this kernel once,
+// and `cap` evaluations also end the loop, so it is bounded whatever the step
+// kernel does.  ctl->reserved[0] counts evaluations, reserved[1] holds the
+// bits of t at the previous one.
 constexpr int kGraphLoopCap = 1 << 24;
-// the cap new loop graphs get (tf_debug_set_graph_loop_cap lowers it so a
-// test can run into it)
+// the step cap of the device-side t_final loops started from now on
+// (tf_debug_set_graph_loop_cap lowers it so a test can run into it)
 static std::atomic<int> g_graph_loop_cap{kGraphLoopCap};
 // the time a tf_time_integration loop starts from: 0 as in the reference
 // (time_integration.py:66); tf_debug_set_loop_start_time changes it so a
@@ -193,6 +196,9 @@ __global__ void loop_cond_kernel(tf_ctl* ctl, cudaGraphConditionalHandle h, int 
     ctl->status = TF_ERR_TIMEOUT;
     active = 0;
   }
+  if (!active && ctl->status == TF_OK && ld_volatile(&ctl->iter) >= cap &&
+      t < ld_volatile(&ctl->t_final))
+    ctl->status = TF_ERR_TIMEOUT;
   ctl->active = active;
   ctl->reserved[0] = evals;
   ctl->reserved[1] = __float_as_int(t);
@@ -616,8 +622,11 @@ static int resolve_tile(const tf_tile_config* tile, int nx, int ny, int nz, unsi
     *loader = tile->loader;
     return TF_OK;
   }
+  // the y-marching tile from 2^17 cells up: below, a step is a few
+  // microseconds of latency and the x-marching tile's shorter chains win
+  // (32^3 4.9 vs 4.5, 48^3 13.7 vs 13.2 Gcell-updates/s)
   const bool fit = !(flags & (TF_FLAG_EXACT | TF_FLAG_OPEN_BOUNDARIES)) && (nz & 1) == 0 &&
-                   nx >= 4;
+                   nx >= 4 && (long long)nx * ny * nz >= (1LL << 17);
   if (fit && overlap_xmarch(ny, nz) >= overlap_ymarch(nz)) {
     *rows = 8;
     *loader = 3;
@@ -803,11 +812,13 @@ static FusedArgs step_args(FusedArgs a, const LoopBufs& b, long long i) {
 }
 
 // The t_final loop as a CUDA graph: {condition, step 1, condition} and then a
-// while node whose body is {even step, condition, odd step, condition}, so
+// while node whose body is an even number of steps and one condition, so
 // every step launch carries its own buffers.  Each step is predicated on the
 // loop condition the previous step's last CTA (or the condition kernel) left
-// in the control block, so a loop that ends after an odd step skips the
-// body's second step.  The kernel arguments bake in the buffers and scalars,
+// in the control block, so the steps of the last body past the end of the
+// loop only launch and exit.  Small grids take 8 steps per body: the
+// per-iteration cost of the while node and the condition kernel (~3 us)
+// then falls on every eighth step instead of every second.  The kernel arguments bake in the buffers and scalars,
 // so executable graphs are cached by (device, arguments, buffers, tile): a
 // repeated call on the same buffers launches the cached graph.  An evicted
 // graph is destroyed at once; CUDA frees it after any in-flight launch
@@ -828,14 +839,19 @@ constexpr size_t kGraphCacheSize = 8;
 static int build_graph_loop(const FusedArgs& a, const LoopBufs& b, int rows, bool exact,
                             tf_ctl* ctl, int cap, cudaGraphExec_t* out);
 
+// steps per while-node body of a t_final loop graph (even)
+static int body_steps(const FusedGeom& g) {
+  return (long long)g.nx * g.ny * g.nz <= (1LL << 22) ? 8 : 2;
+}
+
 static int graph_loop(const FusedArgs& a, const LoopBufs& b, int rows, bool exact, tf_ctl* ctl,
-                      cudaStream_t s) {
+                      int cap, cudaStream_t s) {
   GraphKey k;
   memset(&k, 0, sizeof k);
   TF_TRY(cuda_check(cudaGetDevice(&k.device), "cudaGetDevice"));
   k.rows = rows;
   k.exact = exact ? 1 : 0;
-  k.cap = g_graph_loop_cap.load();
+  k.cap = cap;
   k.a = a;
   k.a.src = nullptr;
   k.a.dst = nullptr;
@@ -924,19 +940,19 @@ static int build_graph_loop(const FusedArgs& a, const LoopBufs& b, int rows, boo
              "cudaStreamUpdateCaptureDependencies"))
       break;
     if (fail(end_capture(), "cudaStreamEndCapture")) break;
-    // the body: steps 2k and 2k + 1, each followed by the condition
+    // the body: steps 2k .. 2k + m - 1, then the condition
     cudaGraph_t body = np.conditional.phGraph_out[0];
     if (fail(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
                                            cudaStreamCaptureModeThreadLocal),
              "cudaStreamBeginCaptureToGraph(body)"))
       break;
     capturing = true;
-    for (int i = 2; i <= 3 && lst == TF_OK; ++i) {
+    const int m = body_steps(a.geo);
+    for (int i = 2; i <= 1 + m && lst == TF_OK; ++i)
       lst = launch_fused(step_args(a, b, i), rows, exact, cs, 1);
-      if (lst == TF_OK) {
-        launch_step(loop_cond_kernel, dim3(1), dim3(1), 0, cs, ctl, h, cap);
-        lst = launch_check("loop_cond_kernel");
-      }
+    if (lst == TF_OK) {
+      launch_step(loop_cond_kernel, dim3(1), dim3(1), 0, cs, ctl, h, cap);
+      lst = launch_check("loop_cond_kernel");
     }
     if (lst != TF_OK) {
       st = lst;
@@ -1284,7 +1300,11 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
   const long long n = (long long)nx * ny * nz;
   const bool exact = (flags & TF_FLAG_EXACT) != 0;
 
-  ctl_init_kernel<<<1, 1, 0, s>>>(ctl, t_final, cfl * dx, max_steps, g_loop_t0.load());
+  // the device-side t_final loop stops its steps after `cap` of them
+  const bool graph = max_steps < 0 && !(flags & TF_FLAG_HOST_LOOP);
+  const int cap = g_graph_loop_cap.load();
+  ctl_init_kernel<<<1, 1, 0, s>>>(ctl, t_final, cfl * dx, graph ? cap : max_steps,
+                                  g_loop_t0.load());
   maxspeed_kernel<<<elementwise_grid(n), 256, 0, s>>>(W_in, n, gamma, ctl, exact ? 0 : 1);
   TF_TRY(launch_check("maxspeed_kernel"));
 
@@ -1308,8 +1328,8 @@ int tf_time_integration(const float* W_in, float* W_out, float* work, tf_ctl* ct
     // step count known: enqueue exactly that many predicated steps
     for (int i = 1; i <= max_steps; ++i)
       TF_TRY(launch_fused(step_args(a, bufs, i), rows, exact, s, loader));
-  } else if (!(flags & TF_FLAG_HOST_LOOP)) {
-    TF_TRY(graph_loop(a, bufs, rows, exact, ctl, s));
+  } else if (graph) {
+    TF_TRY(graph_loop(a, bufs, rows, exact, ctl, cap, s));
   } else {
     // run to t_final: chunks of predicated steps, one host check per chunk
     static thread_local tf_ctl* pinned = nullptr;
