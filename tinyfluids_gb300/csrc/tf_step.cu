@@ -1509,7 +1509,7 @@ extern "C" int tf_time_integration_noalloc(const float* W_in, float* W_out, int 
 
   cudaStream_t s = (cudaStream_t)stream;
   const bool exact = (flags & TF_FLAG_EXACT) != 0;
-  // the tile of tf_time_integration's default (16 rows, heuristic chunk length)
+  // tf_time_integration's built-in tile choice (rows, layout, chunk length)
   int rows, lx, loader;
   TF_TRY(resolve_tile(nullptr, nx, ny, nz, flags, &rows, &lx, &loader));
   // the control block keeps the previous call's contents: re-initialise all of it
