@@ -412,3 +412,26 @@ def test_tma_loop_matches_load_loop(tg):
     a = tg.run_steps(W, dx, GAMMA, 9, tile=(16, 16, "ldg"))
     b = tg.run_steps(W, dx, GAMMA, 9, tile=(16, 16, "tma"))
     assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("shape", [(40, 36, 64), (64, 64, 120)])
+def test_run_steps_inside_user_graph_capture(tg, shape):
+    """A step loop captured into the caller's own CUDA graph (the steps are
+    launched as programmatic dependents of one another) replays to the same
+    bits as the eager loop, twice over, in both tile layouts."""
+    W = dev(random_state(shape, 91))
+    ref = tg.run_steps(W, 0.05, GAMMA, 7)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        tg.run_steps(W, 0.05, GAMMA, 7)  # warm-up outside the capture
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        out = tg.run_steps(W, 0.05, GAMMA, 7)
+    for _ in range(2):
+        out.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(out, ref)
