@@ -194,6 +194,30 @@ int tf_time_integration(const float *W_in, float *W_out, float *work, tf_ctl *ct
                         int max_steps, float fixed_dt, unsigned flags,
                         const tf_tile_config *tile, int *iters_host, void *stream);
 
+/* Device workspace bytes of tf_time_integration_host for `count` states of
+ * nx*ny*nz cells: two slots of three states and one control block per state
+ * (0 for invalid arguments). */
+unsigned long long tf_host_runs_workspace_bytes(int nx, int ny, int nz, int count);
+
+/* time_integration.py:94-128 called with HOST arrays, for a stream of
+ * `count` independent states of one grid size: each W_in_host[k] is copied to
+ * the device, run with exactly tf_time_integration's loop and arguments, and
+ * its final state copied to W_out_host[k].  The copies of one state overlap
+ * the runs of its neighbours (two device slots; one copy stream each way, the
+ * runs on `stream`), so with pinned host memory the stream runs at about the
+ * device's step rate instead of the sum of copy and step times (pageable
+ * memory works, without the overlap).  Blocks until every output is in host
+ * memory.  iters_host (count ints, may be NULL) receives each run's iteration
+ * count; a device-side error is reported with the index of its state.  Inputs
+ * may repeat; an output may share memory with its own or earlier inputs (in
+ * place), not with a later state's input (TF_ERR_ARG).  workspace: device
+ * memory of tf_host_runs_workspace_bytes bytes, 256-byte aligned. */
+int tf_time_integration_host(const float *const *W_in_host, float *const *W_out_host, int count,
+                             int nx, int ny, int nz, float dx, float t_final, float gamma,
+                             float cfl, int max_steps, float fixed_dt, unsigned flags,
+                             const tf_tile_config *tile, void *workspace,
+                             unsigned long long workspace_bytes, int *iters_host, void *stream);
+
 /* Per-sweep form of fluid.py:508-557 (_evolve_state_along_axis), axis 0..2:
  * reads W_in, writes W_out.  TF_FLAG_OPEN_BOUNDARIES applies the
  * fluid.py:571-572 remap to the input (use it for the x sweep only).

@@ -91,6 +91,61 @@ def test_host_side_argument_checks(lib):
                   None, None, None)
 
 
+def test_host_state_runs_check_arguments_before_any_copy(lib):
+    """tf_time_integration_host: workspace size, alignment, pointer lists,
+    output/input overlap and the run's own arguments are rejected before any
+    CUDA call (fake addresses are never dereferenced)."""
+    from tinyfluids_gb300 import _lib
+    sb = (5 * 4 * 32 ** 3 + 255) // 256 * 256
+    assert lib.tf_host_runs_workspace_bytes(32, 32, 32, 3) == 6 * sb + 256
+    assert lib.tf_host_runs_workspace_bytes(0, 32, 32, 3) == 0
+    assert lib.tf_host_runs_workspace_bytes(32, 32, 32, 0) == 0
+    nbytes = 5 * 4 * 32 ** 3
+    ins = (ctypes.c_void_p * 2)(0x10000000, 0x20000000)
+    outs = (ctypes.c_void_p * 2)(0x30000000, 0x40000000)
+    ws, wsb = ctypes.c_void_p(0x50000000), 6 * sb + 256
+
+    def run(i=ins, o=outs, count=2, w=ws, wb=wsb, dx=0.1, tf=0.2, ms=-1, flags=0):
+        with pytest.raises(_lib.TinyfluidsError) as e:
+            _lib.call("tf_time_integration_host", i, o, count, 32, 32, 32, dx, tf, 5 / 3, 0.4,
+                      ms, 0.0, flags, None, w, wb, None, None)
+        assert e.value.status == 1, str(e.value)
+        return str(e.value)
+
+    run(count=0)
+    run(i=None)
+    run(w=None)
+    assert "needed" in run(wb=wsb - 1)
+    run(w=ctypes.c_void_p(0x50000010))  # not 256-byte aligned
+    run(i=(ctypes.c_void_p * 2)(0x10000000, None))
+    # state 0's output overlaps state 1's input (copied in while 0 is copied out)
+    assert "overlaps" in run(o=(ctypes.c_void_p * 2)(0x20000000 + nbytes - 4, 0x40000000))
+    run(dx=0.0)
+    run(tf=float("inf"))  # unbounded loop
+    with pytest.raises(_lib.TinyfluidsError):  # open boundaries need 2 cells per axis
+        _lib.call("tf_time_integration_host", ins, outs, 2, 1, 32, 32, 0.1, 0.2, 5 / 3, 0.4,
+                  -1, 0.0, 1, None, ws, wsb, None, None)
+
+
+def test_host_state_api_validates_before_launch():
+    import torch
+    import tinyfluids_gb300 as tg
+    good = torch.zeros(5, 4, 4, 4)
+    with pytest.raises(ValueError):
+        tg.time_integration_host([], 0.1, 0.2, 5 / 3, False)
+    with pytest.raises(TypeError):
+        tg.time_integration_host([good, torch.zeros(5, 4, 4, 4, dtype=torch.float64)], 0.1, 0.2,
+                                 5 / 3, False)
+    with pytest.raises(ValueError):  # shapes differ
+        tg.time_integration_host([good, torch.zeros(5, 4, 4, 5)], 0.1, 0.2, 5 / 3, False)
+    with pytest.raises(ValueError):  # non-contiguous
+        tg.time_integration_host([torch.zeros(5, 4, 4, 8)[..., ::2]], 0.1, 0.2, 5 / 3, False)
+    with pytest.raises(ValueError):  # out of the wrong length
+        tg.time_integration_host([good], 0.1, 0.2, 5 / 3, False, out=[good, good])
+    with pytest.raises(ValueError):
+        tg.time_integration_host([good], 0.1, 0.2, 5 / 3, False, num_steps=-1)
+
+
 def test_product_library_is_not_the_checked_build(lib):
     assert lib.tf_debug_checked() == 0
     assert lib.tf_debug_oob_count() == -1

@@ -74,6 +74,10 @@ SIGNATURES = {
                                      c_float, c_int, c_uint, vp]),
     "tf_time_integration_noalloc": (c_int, [vp, vp, c_int, c_int, c_int, c_float, c_float,
                                             c_float, c_float, c_int, c_float, c_uint, vp, vp]),
+    "tf_host_runs_workspace_bytes": (c_ull, [c_int, c_int, c_int, c_int]),
+    "tf_time_integration_host": (c_int, [vp, vp, c_int, c_int, c_int, c_int, c_float, c_float,
+                                         c_float, c_float, c_int, c_float, c_uint, vp, vp, c_ull,
+                                         vp, vp]),
     "tf_batch_workspace_bytes": (c_ull, [c_int]),
     "tf_batch_prepare": (c_int, [vp, c_int, vp, vp, c_ull, vp]),
     "tf_batch_run": (c_int, [vp, c_int, c_int, vp]),

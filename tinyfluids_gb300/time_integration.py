@@ -65,6 +65,79 @@ def step(primitive_state, grid_spacing, gamma, C_CFL=0.4, handle_boundaries=Fals
     return W, ctl.view(torch.float32)[CTL_T].clone()
 
 
+def time_integration_host(primitive_states, grid_spacing, t_final, gamma, handle_boundaries,
+                          *, num_steps=None, C_CFL=0.4, dt=None, exact=None, tile=None,
+                          out=None, device=None):
+    """time_integration.py:94-128 for host-resident states: each CPU state of
+    ``primitive_states`` (a list of [5, nx, ny, nz] float32 CPU tensors of one
+    shape, or one such tensor) is copied to the GPU, run with exactly
+    ``time_integration``'s loop (to ``t_final``, or ``num_steps`` steps when
+    given) and copied back.  The copies of one state overlap the runs of its
+    neighbours, so for pinned host tensors a list of states runs at about the
+    device's step rate.  Returns ``(states, num_iterations)``: lists of CPU
+    tensors (pinned; ``out`` may name them, including the inputs themselves
+    for an in-place update) and ints.  Blocks until the outputs are in host
+    memory."""
+    single = isinstance(primitive_states, torch.Tensor)
+    states = [primitive_states] if single else list(primitive_states)
+    if not states:
+        raise ValueError("no states given")
+    shape = None
+    for i, st in enumerate(states):
+        if not isinstance(st, torch.Tensor) or st.dtype != torch.float32:
+            raise TypeError(f"state {i} must be a float32 torch.Tensor")
+        if st.dim() != 4 or st.shape[0] != 5 or min(st.shape[1:]) < 1:
+            raise TypeError(f"state {i} must have shape [5, nx, ny, nz], got {tuple(st.shape)}")
+        if st.is_cuda:
+            raise ValueError(f"state {i} is on the GPU: use time_integration for device states")
+        if not st.is_contiguous():
+            raise ValueError(f"state {i} must be contiguous")
+        if shape is None:
+            shape = tuple(st.shape)
+        elif tuple(st.shape) != shape:
+            raise ValueError(f"state {i} has shape {tuple(st.shape)}, state 0 {shape}")
+    if num_steps is None:
+        max_steps, tf = -1, float(t_final)
+    else:
+        if int(num_steps) < 0:
+            raise ValueError("num_steps must be >= 0")
+        max_steps = int(num_steps)
+        tf = math.inf if t_final is None else float(t_final)
+    fixed = 0.0 if dt is None else float(dt)
+    if dt is not None and not (fixed > 0 and math.isfinite(fixed)):
+        raise ValueError("a fixed dt must be finite and > 0")
+    if out is None:
+        outs = [torch.empty(shape, dtype=torch.float32, pin_memory=True) for _ in states]
+    else:
+        outs = [out] if isinstance(out, torch.Tensor) else list(out)
+        if len(outs) != len(states):
+            raise ValueError("out must hold one tensor per state")
+        for i, o in enumerate(outs):
+            if (not isinstance(o, torch.Tensor) or o.is_cuda or o.dtype != torch.float32
+                    or tuple(o.shape) != shape or not o.is_contiguous()):
+                raise ValueError(f"out[{i}] must be a contiguous float32 CPU tensor of shape "
+                                 f"{shape}")
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else \
+        torch.device(device)
+    _, nx, ny, nz = shape
+    n = len(states)
+    with torch.cuda.device(dev):
+        lib = _lib.load()
+        nbytes = int(lib.tf_host_runs_workspace_bytes(nx, ny, nz, n))
+        if nbytes == 0:
+            raise ValueError(f"invalid grid {shape[1:]}")
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        ins = (_lib.vp * n)(*[st.data_ptr() for st in states])
+        ous = (_lib.vp * n)(*[o.data_ptr() for o in outs])
+        its = (_lib.c_int * n)()
+        _lib.call("tf_time_integration_host", ins, ous, n, nx, ny, nz, float(grid_spacing), tf,
+                  _scalar(gamma, "gamma"), _scalar(C_CFL, "C_CFL"), max_steps, fixed,
+                  _flags(handle_boundaries, exact), _tile_arg(tile, None, exact), ws.data_ptr(),
+                  nbytes, its, torch.cuda.current_stream(dev).cuda_stream)
+    iters = list(its)
+    return (outs[0], iters[0]) if single else (outs, iters)
+
+
 def _run(primitive_state, grid_spacing, gamma, t_final, max_steps, fixed_dt,
          handle_boundaries, C_CFL, exact, tile, wait, host_loop=False):
     W = check_state(primitive_state)
