@@ -309,6 +309,27 @@ def test_overpressure_64_accuracy_vs_fp64(tg, oracle_lib):
     assert e_fast_l1 <= 2 * e_ref_l1 and e_fast_inf <= 2 * e_ref_inf
 
 
+@pytest.mark.parametrize("n", [64, 128])
+def test_reference_benchmark_accuracy_vs_fp64(tg, oracle_lib, n):
+    """The reference's own benchmark state (setup_ics(n, n//16), open
+    boundaries) over its golden number of steps to t = 0.2: the fast path's
+    density error against the FP64 oracle is within 2x the reference float32
+    scheme's, and the exact path equals the float32 oracle bit for bit."""
+    W, dx = tg.setup_ics(n, n // 16)
+    steps = GOLDEN["counts"][str(n)]
+    W0 = host(W)
+    ref32, _ = oracle_lib.run_steps(W0, dx, GAMMA, steps, True)
+    ref64, _ = oracle_lib.run_steps(W0.astype(np.float64), dx, GAMMA, steps, True)
+    fast = host(tg.run_steps(W, dx, GAMMA, steps, True))
+    exact = host(tg.run_steps(W, dx, GAMMA, steps, True, exact=True))
+    assert np.array_equal(exact, ref32)
+    e_ref = np.abs(ref32[0] - ref64[0])
+    e_fast = np.abs(fast[0] - ref64[0])
+    print(f"{n}^3 density error vs FP64: reference-f32 L1 {e_ref.mean():.3e} "
+          f"Linf {e_ref.max():.3e}; fast L1 {e_fast.mean():.3e} Linf {e_fast.max():.3e}")
+    assert e_fast.mean() <= 2 * e_ref.mean() and e_fast.max() <= 2 * e_ref.max()
+
+
 @pytest.mark.parametrize("host_loop", [False, True])
 def test_nonfinite_state_is_reported(tg, host_loop):
     W = random_state((8, 8, 8), 1)
