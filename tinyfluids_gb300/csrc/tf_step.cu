@@ -772,8 +772,10 @@ static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_
   }
   if (a.totals) {
     TF_DISPATCH_ROWS(rows, NWP, {
-      if (exact) launch_step(fused_step_kernel<ExactPair, NWP, true>, grid, dim3(NWP * 32), 0, s, a);
-      else launch_step(fused_step_kernel<FastPair, NWP, true>, grid, dim3(NWP * 32), 0, s, a);
+      if (exact)
+        launch_step(fused_step_kernel<ExactPair, NWP, true>, grid, dim3(NWP * 32), 0, s, a);
+      else
+        launch_step(fused_step_kernel<FastPair, NWP, true>, grid, dim3(NWP * 32), 0, s, a);
     });
     return launch_check("fused_step_kernel (diagnostics)");
   }
@@ -782,7 +784,8 @@ static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_
       return set_error(TF_ERR_UNSUPPORTED,
                        "conserved input/output: fast arithmetic and 16-row tiles only");
     if (vs < (1ull << 31) && !g_force_64bit.load())
-      launch_step(fused_step_kernel<FastPairConserved, 8, false, true>, grid, dim3(8 * 32), 0, s, a);
+      launch_step(fused_step_kernel<FastPairConserved, 8, false, true>, grid, dim3(8 * 32), 0, s,
+                  a);
     else
       launch_step(fused_step_kernel<FastPairConserved, 8>, grid, dim3(8 * 32), 0, s, a);
     return launch_check("fused_step_kernel (conserved)");
