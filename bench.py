@@ -323,6 +323,7 @@ def run_gpu(args):
             e2e_ms.append(a.elapsed_time(b))
     e2e_value, e2e = replicas.job_throughput(cells, K * R, min(e2e_ms), world, dev)
     del Oh2, outs_h
+    torch.cuda.empty_cache()  # the host-run workspace (six states) is not needed again
 
     if rank != 0:
         return 0
