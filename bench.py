@@ -154,10 +154,11 @@ class ClockSampler:
                 "samples": len(win)}
 
 
-def cpu_baseline(n, seconds_budget, steps_cap):
+def cpu_baseline(n, seconds_budget, steps_cap, warmup=3):
     """The C restatement of the reference step (all host threads) on an n^3
-    shear layer; times up to steps_cap steps, bounded by the time budget.
-    The returned dict's "steps" is the number of steps timed."""
+    shear layer: `warmup` untimed steps, then up to steps_cap timed steps,
+    bounded by the time budget.  The returned dict's "steps" is the number of
+    steps timed."""
     import numpy as np
     from oracle import build as ob
     from oracle import fluid_c
@@ -165,19 +166,20 @@ def cpu_baseline(n, seconds_budget, steps_cap):
     ob.build()
     threads = fluid_c.max_threads()
     W, dx = ics_np.shear_layer(n, seed=0)
-    # warm-up: one step (also measures the per-step cost)
+    # warm-up steps (also measure the per-step cost)
+    warmup = max(1, int(warmup))
     t0 = time.perf_counter()
-    W1, _ = fluid_c.run_steps(W, dx, GAMMA, 1)
-    per = time.perf_counter() - t0
+    W1, _ = fluid_c.run_steps(W, dx, GAMMA, warmup)
+    per = (time.perf_counter() - t0) / warmup
     k = int(max(1, min(steps_cap, seconds_budget // max(per, 1e-9))))
     t0 = time.perf_counter()
     fluid_c.run_steps(W1, dx, GAMMA, k)
     el = time.perf_counter() - t0
     del np
     return {"value": n ** 3 * k / el / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-            "steps": k, "seconds": el,
-            "sample": f"{k} CFL steps of the {n}^3 shear layer timed (after 1 untimed warm-up "
-                      f"step), C restatement of fluid.py/time_integration.py, "
+            "steps": k, "warmup": warmup, "seconds": el,
+            "sample": f"{k} CFL steps of the {n}^3 shear layer timed (after {warmup} untimed "
+                      f"warm-up steps), C restatement of fluid.py/time_integration.py, "
                       f"{threads} OpenMP threads"}
 
 
@@ -186,9 +188,9 @@ def run_reference(args):
     if rank != 0:
         return 0
     # every requested step is timed unless that would take more than ~90 s
-    cb = cpu_baseline(args.n, 90.0, max(1, args.steps))
+    cb = cpu_baseline(args.n, 90.0, max(1, args.steps), warmup=max(3, args.warmup))
     line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
-            "n_gpus": args.gpus, "steps": cb["steps"], "warmup": 1,
+            "n_gpus": args.gpus, "steps": cb["steps"], "warmup": cb["warmup"],
             "steps_requested": args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "ms_per_step": 1e3 * cb["seconds"] / cb["steps"],
