@@ -311,7 +311,7 @@ def run_gpu(args):
     Oh2 = torch.empty_like(Wh).pin_memory()
     outs_h = [Oh if k % 2 == 0 else Oh2 for k in range(R)]
     e2e_ms = []
-    for rep in range(3):
+    for rep in range(4):
         barrier()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
