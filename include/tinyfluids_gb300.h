@@ -73,12 +73,13 @@ typedef struct tf_ctl {
 } tf_ctl;
 
 /* Tile of the fused step kernel; NULL = built-in choice: the y-marching
- * 8-row tile for a fast (or diagnostics / conserved) step on a periodic grid
- * with an even nz and at least 2^17 cells where it computes no more cells
- * than the x-marching tile, else the x-marching tile (8 rows up to 2^21
- * cells, 16 above; always 16 for conserved input or output); the chunk length (lx) for about nine waves
- * of resident CTAs in chunks of >= 16 planes (y-marching: <= 64), shorter
- * chunks for grids that would not fill one wave.  tf_resolve_tile reports the
+ * 8-row tile for a fast (or diagnostics / conserved) step on a grid with an
+ * even nz and at least 2^17 cells (open boundaries: a fast step on at least
+ * 2^27 cells) where it computes no more cells than the x-marching tile, else
+ * the x-marching tile (8 rows up to 2^21 cells, 16 above; always 16 for
+ * conserved input or output); the chunk length (lx) for about nine waves of
+ * resident CTAs in chunks of >= 16 planes (y-marching: <= 64), shorter chunks
+ * for grids that would not fill one wave.  tf_resolve_tile reports the
  * choice. */
 typedef struct tf_tile_config {
   int rows;    /* x-marching: grid rows (y) per tile incl. the 1-cell ring: 8, 16 or 32

@@ -169,9 +169,9 @@ def test_python_api_validates_before_launch():
 def test_tile_choice(lib):
     """The built-in tile choice (no GPU needed: dimensions and flags only):
     the y-marching 8-row tile where it computes no more cells than the
-    x-marching 16-row tile (fast arithmetic, periodic, even nz, 2^17 cells or
-    more), else the x-marching tile (8 rows up to 128^3 cells, 16 above);
-    explicit tiles are taken as given."""
+    x-marching 16-row tile (fast arithmetic, even nz, 2^17 cells or more;
+    open boundaries from 2^27 cells), else the x-marching tile (8 rows up to
+    128^3 cells, 16 above); explicit tiles are taken as given."""
     import tinyfluids_gb300 as tg
     assert tg.resolved_tile((512, 512, 512), exact=False)[::2] == (8, "ym")
     assert tg.resolved_tile((768, 768, 768), exact=False)[::2] == (8, "ym")
@@ -181,7 +181,9 @@ def test_tile_choice(lib):
     assert tg.resolved_tile((128, 128, 128), exact=False)[::2] == (8, "ldg")
     assert tg.resolved_tile((256, 256, 256), exact=False) == (16, 32, "ldg")
     assert tg.resolved_tile((512, 512, 512), exact=True)[::2] == (16, "ldg")
-    assert tg.resolved_tile((512, 512, 512), True, exact=False)[::2] == (16, "ldg")
+    assert tg.resolved_tile((512, 512, 512), True, exact=False)[::2] == (8, "ym")
+    assert tg.resolved_tile((384, 384, 384), True, exact=False)[::2] == (16, "ldg")
+    assert tg.resolved_tile((512, 512, 2), True, exact=False)[::2] == (8, "ldg")
     assert tg.resolved_tile((512, 512, 511), exact=False)[::2] == (16, "ldg")
     rows, lx, lay = tg.resolved_tile((512, 512, 512), exact=False)
     assert 16 <= lx <= 64

@@ -44,6 +44,17 @@ def test_tile_shapes_agree(tg, shear):
         assert torch.equal(tg._evolve_state(W, dx, dt, GAMMA, tile=tile), ref), tile
 
 
+def test_open_boundary_tiles_agree(tg, shear):
+    """Open boundaries at 512^3 (the built-in choice: the y-marching tile
+    with its z-edge pair fix-up) equal the x-marching tile bit for bit, and
+    one exact step with open boundaries equals the exact x-marching step."""
+    W, dx, dt = shear
+    assert tg.resolved_tile((N, N, N), True, exact=False)[2] == "ym"
+    ref = tg._evolve_state(W, dx, dt, GAMMA, True, tile=(16, 0, "ldg"))
+    for tile in (None, (8, 0, "ym"), (8, 37, "ym"), (16, 0, "ym")):
+        assert torch.equal(tg._evolve_state(W, dx, dt, GAMMA, True, tile=tile), ref), tile
+
+
 def test_fused_equals_three_sweeps(tg, shear):
     W, dx, dt = shear
     fused = tg._evolve_state(W, dx, dt, GAMMA)

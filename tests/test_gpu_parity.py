@@ -183,7 +183,8 @@ def test_fast_step_independent_of_tile_shape(tg, shape):
 
 
 YM_SHAPES = [(1, 1, 1), (2, 3, 5), (5, 7, 33), (4, 9, 60), (9, 13, 62), (13, 5, 121),
-             (40, 31, 64), (3, 64, 29), (64, 15, 2), (17, 2, 130)]
+             (40, 31, 64), (3, 64, 29), (64, 15, 2), (17, 2, 130), (6, 5, 4), (5, 6, 6),
+             (7, 3, 120), (3, 4, 122)]
 
 
 @pytest.mark.parametrize("shape", YM_SHAPES)

@@ -148,11 +148,15 @@ struct ShflLower {
 // One CTA-tile of the y-marching fused step: x rows x0 .. x0+NW-1 (tile tx),
 // the 64 z cells 60*tz-2 .. 60*tz+61 (tile tz) of which lanes 1..30 store
 // 60*tz .. 60*tz+59, planes y0 .. y0+ly-1 (chunk ty, ly = G.lx).  Lane pairs
-// start at even z: with VEC (periodic wrap, even nz, 8-byte aligned states)
-// every pair moves as one 8-byte access.  Returns this thread's running
-// maximum of the stored cells' wave speeds (0 for threads that store nothing).
-// DIAG and VP as in fused_tile.
-template <class P, int NW, bool DIAG = false, bool VP = false, bool VEC = false>
+// start at even z: with VEC (even nz, 8-byte aligned states) every pair moves
+// as one 8-byte access.  VEC 1: periodic wrap; VEC 2: open boundaries, where
+// the clamp of the source index to [1, nz-2] turns exactly two pairs into
+// repeats of one cell, (0,1) into (1,1) and (nz-2,nz-1) into (nz-2,nz-2):
+// those pairs load whole from their wrapped address and are fixed up after the
+// load (nz >= 4).  Returns this thread's running maximum of the stored cells'
+// wave speeds (0 for threads that store nothing).  DIAG and VP as in
+// fused_tile.
+template <class P, int NW, bool DIAG = false, bool VP = false, int VEC = 0>
 __device__ __forceinline__ float fused_tile_ym(const float* __restrict__ src,
                                                float* __restrict__ dst, const FusedGeom& G,
                                                int tx, int tz, int ty,
@@ -175,7 +179,15 @@ __device__ __forceinline__ float fused_tile_ym(const float* __restrict__ src,
   const Off nz = (Off)G.nz;
   const Off xstride = (Off)G.ny * (Off)G.nz;
   const size_t vstride = (size_t)G.nx * G.ny * G.nz;
-  const Off zsa = (Off)src_index(za, G.nz, open), zsb = (Off)src_index(zb, G.nz, open);
+  // pairs move from their wrapped address (the checked build reads cells one
+  // by one, through the full source-index map)
+  constexpr bool kPairAddr = VEC != 0 && !TF_CHECKED;
+  const int zwa = wrap_index(za, G.nz);
+  const Off zsa = (Off)(kPairAddr ? zwa : src_index(za, G.nz, open));
+  const Off zsb = (Off)(kPairAddr ? zwa + 1 : src_index(zb, G.nz, open));
+  // open boundaries: does this warp hold one of the two pairs the clamp
+  // turns into repeated cells (warp-uniform)
+  const bool zfix = VEC == 2 && __any_sync(0xffffffffu, zwa == 0 || zwa == G.nz - 2);
   const Off rs = (Off)src_index(x, G.nx, open) * xstride;
   const Off ra = rs + zsa;
   const Off rb = rs + zsb;
@@ -251,6 +263,17 @@ __device__ __forceinline__ float fused_tile_ym(const float* __restrict__ src,
     const float2(*slot)[32] = sm.ring[stage_of(y)][halo ? hslot : w + 1];
 #pragma unroll
     for (int i = 0; i < 5; ++i) v[i] = slot[i][lane];
+    if constexpr (VEC == 2) {
+      if (zfix) {  // only the warps of the two z-edge tiles
+        const int zw = wrap_index(tz * kYmZ - 2 + 2 * lane, G.nz);
+        const bool lo = zw == 0, hi = zw == G.nz - 2;  // (0,1) -> (1,1); (nz-2,nz-1) -> (nz-2,nz-2)
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+          if (lo) v[i].x = v[i].y;
+          if (hi) v[i].y = v[i].x;
+        }
+      }
+    }
   };
   // this plane's copies have landed; the next plane's may still be in flight
   auto wait_plane = []() { cp_async_wait_prev(); };

@@ -396,7 +396,7 @@ __global__ void TF_FUSED_BOUNDS(NWP) fused_step_kernel(const __grid_constant__ F
 
 // The y-marching fused step (fused_tile_ym): NW x rows per CTA, grid
 // (x tiles, z tiles, y chunks).
-template <class P, int NW, bool DIAG = false, bool VP = false, bool VEC = false>
+template <class P, int NW, bool DIAG = false, bool VP = false, int VEC = 0>
 __global__ void __launch_bounds__(NW * 32, min_ctas_per_sm(NW))
     fused_step_ym_kernel(const __grid_constant__ FusedArgs a) {
   extern __shared__ __align__(16) unsigned char ym_smem[];
@@ -624,9 +624,15 @@ static int resolve_tile(const tf_tile_config* tile, int nx, int ny, int nz, unsi
   }
   // the y-marching tile from 2^17 cells up: below, a step is a few
   // microseconds of latency and the x-marching tile's shorter chains win
-  // (32^3 4.9 vs 4.5, 48^3 13.7 vs 13.2 Gcell-updates/s)
-  const bool fit = !(flags & (TF_FLAG_EXACT | TF_FLAG_OPEN_BOUNDARIES)) && (nz & 1) == 0 &&
-                   nx >= 4 && (long long)nx * ny * nz >= (1LL << 17);
+  // (32^3 4.9 vs 4.5, 48^3 13.7 vs 13.2 Gcell-updates/s); with open
+  // boundaries (its 8-byte pairs fixed up at the z edges) from 2^27 cells
+  // (512^3 86.6 vs 84.3, 768^3 88.7 vs 88.1; 384^3 79.4 vs 82.3)
+  const long long cells = (long long)nx * ny * nz;
+  const bool open = (flags & TF_FLAG_OPEN_BOUNDARIES) != 0;
+  const bool fit =
+      !(flags & TF_FLAG_EXACT) && (nz & 1) == 0 && nx >= 4 && cells >= (1LL << 17) &&
+      (!open || (cells >= (1LL << 27) && nz >= 4 &&
+                 !(flags & (TF_FLAG_IN_CONSERVED | TF_FLAG_OUT_CONSERVED))));
   if (fit && overlap_xmarch(ny, nz) >= overlap_ymarch(nz)) {
     *rows = 8;
     *loader = 3;
@@ -677,11 +683,12 @@ static void launch_step(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t sm
 }
 
 // Template arguments of one y-marching kernel instantiation.
-template <class P_, int NW_, bool DIAG_, bool VP_, bool VEC_ = false>
+template <class P_, int NW_, bool DIAG_, bool VP_, int VEC_ = 0>
 struct YmTag {
   using P = P_;
   static constexpr int nw = NW_;
-  static constexpr bool diag = DIAG_, vp = VP_, vec = VEC_;
+  static constexpr bool diag = DIAG_, vp = VP_;
+  static constexpr int vec = VEC_;
 };
 
 // Dynamic shared memory of the y-marching kernel with NW warps.
@@ -725,8 +732,11 @@ static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_
                     7) == 0 && (vs & 1) == 0 && (a.geo.nz & 1) == 0;
     const dim3 g(a.geo.tiles_x, a.geo.tiles_z, a.geo.tiles_y);
     const bool vp = vs < (1ull << 31) && !g_force_64bit.load();
-    // 8-byte pair accesses: periodic wrap keeps every pair whole when nz is even
+    // 8-byte pair accesses: periodic wrap keeps every pair whole when nz is
+    // even; with open boundaries the fast step fixes up the two pairs the
+    // clamp changes (nz >= 4)
     const bool vec = a.geo.pairs8 && !a.geo.open_bc;
+    const bool vec_open = a.geo.pairs8 && a.geo.open_bc && a.geo.nz >= 4;
     int st = TF_OK;
     auto go = [&](auto nw_c) {
       constexpr int NW = decltype(nw_c)::value;
@@ -741,17 +751,19 @@ static int launch_fused(const FusedArgs& a_in, int rows, bool exact, cudaStream_
         if (exact) launch(YmTag<ExactPair, NW, true, false>{});
         else launch(YmTag<FastPair, NW, true, false>{});
       } else if (a.conserved_io) {
-        if (vp && vec) launch(YmTag<FastPairConserved, NW, false, true, true>{});
+        if (vp && vec) launch(YmTag<FastPairConserved, NW, false, true, 1>{});
         else if (vp) launch(YmTag<FastPairConserved, NW, false, true>{});
         else launch(YmTag<FastPairConserved, NW, false, false>{});
       } else if (exact) {
         launch(YmTag<ExactPair, NW, false, false>{});
       } else if (vp && vec) {
-        launch(YmTag<FastPair, NW, false, true, true>{});
+        launch(YmTag<FastPair, NW, false, true, 1>{});
+      } else if (vp && vec_open) {
+        launch(YmTag<FastPair, NW, false, true, 2>{});
       } else if (vp) {
         launch(YmTag<FastPair, NW, false, true>{});
       } else if (vec) {
-        launch(YmTag<FastPair, NW, false, false, true>{});
+        launch(YmTag<FastPair, NW, false, false, 1>{});
       } else {
         launch(YmTag<FastPair, NW, false, false>{});
       }
