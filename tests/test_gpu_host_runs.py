@@ -77,6 +77,9 @@ def test_in_place_pageable_and_repeated_inputs(tg):
     outs, _ = tg.time_integration_host([one] * 3, 0.05, None, GAMMA, False, num_steps=3)
     for o in outs:
         assert torch.equal(o, refs[0])
+    # a numpy array, alone
+    o, it = tg.time_integration_host(base[1].numpy(), 0.05, None, GAMMA, False, num_steps=3)
+    assert it == 3 and torch.equal(o, refs[1])
 
 
 def test_device_errors_name_their_state(tg):

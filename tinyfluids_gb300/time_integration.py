@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import math
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -69,8 +70,8 @@ def time_integration_host(primitive_states, grid_spacing, t_final, gamma, handle
                           *, num_steps=None, C_CFL=0.4, dt=None, exact=None, tile=None,
                           out=None, device=None):
     """time_integration.py:94-128 for host-resident states: each CPU state of
-    ``primitive_states`` (a list of [5, nx, ny, nz] float32 CPU tensors of one
-    shape, or one such tensor) is copied to the GPU, run with exactly
+    ``primitive_states`` (a list of [5, nx, ny, nz] float32 CPU tensors or
+    numpy arrays of one shape, or one such state) is copied to the GPU, run with exactly
     ``time_integration``'s loop (to ``t_final``, or ``num_steps`` steps when
     given) and copied back.  The copies of one state overlap the runs of its
     neighbours, so for pinned host tensors a list of states runs at about the
@@ -78,10 +79,12 @@ def time_integration_host(primitive_states, grid_spacing, t_final, gamma, handle
     tensors (pinned; ``out`` may name them, including the inputs themselves
     for an in-place update) and ints.  Blocks until the outputs are in host
     memory."""
-    single = isinstance(primitive_states, torch.Tensor)
+    single = isinstance(primitive_states, (torch.Tensor, np.ndarray))
     states = [primitive_states] if single else list(primitive_states)
     if not states:
         raise ValueError("no states given")
+    # numpy arrays are viewed, not copied
+    states = [torch.from_numpy(st) if isinstance(st, np.ndarray) else st for st in states]
     shape = None
     for i, st in enumerate(states):
         if not isinstance(st, torch.Tensor) or st.dtype != torch.float32:
