@@ -152,8 +152,8 @@ struct ShflLower {
 // as one 8-byte access.  VEC 1: periodic wrap; VEC 2: open boundaries, where
 // the clamp of the source index to [1, nz-2] turns exactly two pairs into
 // repeats of one cell, (0,1) into (1,1) and (nz-2,nz-1) into (nz-2,nz-2):
-// those pairs load whole from their wrapped address and are fixed up after the
-// load (nz >= 4).  Returns this thread's running maximum of the stored cells'
+// those pairs load whole from their wrapped address and are fixed up after
+// the y sweep (nz >= 4).  Returns this thread's running maximum of the stored cells'
 // wave speeds (0 for threads that store nothing).  DIAG and VP as in
 // fused_tile.
 template <class P, int NW, bool DIAG = false, bool VP = false, int VEC = 0>
@@ -263,17 +263,6 @@ __device__ __forceinline__ float fused_tile_ym(const float* __restrict__ src,
     const float2(*slot)[32] = sm.ring[stage_of(y)][halo ? hslot : w + 1];
 #pragma unroll
     for (int i = 0; i < 5; ++i) v[i] = slot[i][lane];
-    if constexpr (VEC == 2) {
-      if (zfix) {  // only the warps of the two z-edge tiles
-        const int zw = wrap_index(tz * kYmZ - 2 + 2 * lane, G.nz);
-        const bool lo = zw == 0, hi = zw == G.nz - 2;  // (0,1) -> (1,1); (nz-2,nz-1) -> (nz-2,nz-2)
-#pragma unroll
-        for (int i = 0; i < 5; ++i) {
-          if (lo) v[i].x = v[i].y;
-          if (hi) v[i].y = v[i].x;
-        }
-      }
-    }
   };
   // this plane's copies have landed; the next plane's may still be in flight
   auto wait_plane = []() { cp_async_wait_prev(); };
@@ -387,6 +376,23 @@ __device__ __forceinline__ float fused_tile_ym(const float* __restrict__ src,
     P::hll(cur, nxt, fp);  // face y + 1/2
     V2 s2[5];
     P::update(cur, fm, fp, s2, K);
+    if constexpr (VEC == 2) {
+      // open boundaries: a cell whose input the clamp replaces by its z
+      // neighbour's, z = 0 by z = 1 and z = nz-1 by nz-2, has x and y
+      // neighbours replaced the same way, so after the x and y sweeps it
+      // equals that neighbour bit for bit; the pair loaded whole from the
+      // wrapped address takes it now, before the z sweep (its x and y sweeps
+      // ran on the unclamped cell and reach no other cell)
+      if (zfix) {
+        const int zw = wrap_index(tz * kYmZ - 2 + 2 * lane, G.nz);
+        const bool lo = zw == 0, hi = zw == G.nz - 2;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+          if (lo) s2[i].x = s2[i].y;
+          if (hi) s2[i].y = s2[i].x;
+        }
+      }
+    }
     // ---- z sweep ----
     Cell2 cz;
     P::template derive<3>(s2, cz, K);

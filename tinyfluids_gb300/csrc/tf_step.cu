@@ -626,7 +626,7 @@ static int resolve_tile(const tf_tile_config* tile, int nx, int ny, int nz, unsi
   // microseconds of latency and the x-marching tile's shorter chains win
   // (32^3 4.9 vs 4.5, 48^3 13.7 vs 13.2 Gcell-updates/s); with open
   // boundaries (its 8-byte pairs fixed up at the z edges) from 2^27 cells
-  // (512^3 86.6 vs 84.3, 768^3 88.7 vs 88.1; 384^3 79.4 vs 82.3)
+  // (512^3 87.5 vs 84.3, 768^3 88.7 vs 88.1; 384^3 79.4 vs 82.3)
   const long long cells = (long long)nx * ny * nz;
   const bool open = (flags & TF_FLAG_OPEN_BOUNDARIES) != 0;
   const bool fit =
