@@ -21,6 +21,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <algorithm>
+#include <utility>
 #include <vector>
 
 #include "tf_host.h"
@@ -85,13 +87,21 @@ extern "C" int tf_time_integration_host(const float* const* W_in_host, float* co
   if (ts != TF_OK) return ts;
   const size_t bytes = 5ull * sizeof(float) * (size_t)nx * ny * nz;
   // an output is copied back while later inputs may still be copied in: it
-  // may share memory with its own or earlier inputs (in place), not later ones
-  for (int k = 0; k < count; ++k) {
-    const uintptr_t o = reinterpret_cast<uintptr_t>(W_out_host[k]);
-    for (int j = k + 1; j < count; ++j) {
-      const uintptr_t i = reinterpret_cast<uintptr_t>(W_in_host[j]);
-      if (o < i + bytes && i < o + bytes)
-        return set_error(TF_ERR_ARG, "output %d overlaps the input of later state %d", k, j);
+  // may share memory with its own or earlier inputs (in place), not later
+  // ones.  Inputs sorted by address: the ones overlapping an output start
+  // within `bytes` of it on either side.
+  {
+    std::vector<std::pair<uintptr_t, int>> ins((size_t)count);
+    for (int j = 0; j < count; ++j) ins[(size_t)j] = {reinterpret_cast<uintptr_t>(W_in_host[j]), j};
+    std::sort(ins.begin(), ins.end());
+    for (int k = 0; k < count; ++k) {
+      const uintptr_t o = reinterpret_cast<uintptr_t>(W_out_host[k]);
+      const uintptr_t lo = o >= bytes ? o - bytes + 1 : 0;
+      auto it = std::lower_bound(ins.begin(), ins.end(), std::make_pair(lo, -1));
+      for (; it != ins.end() && it->first < o + bytes; ++it)
+        if (it->second > k)
+          return set_error(TF_ERR_ARG, "output %d overlaps the input of later state %d", k,
+                           it->second);
     }
   }
   unsigned char* base = static_cast<unsigned char*>(workspace);
