@@ -170,7 +170,8 @@ __device__ __forceinline__ float fused_tile_ym(const float* __restrict__ src,
   // the warp index through a shuffle from lane 0: provably the same in every
   // lane, so branches on it need no convergence barriers (measured +0.5%)
   const int w = __shfl_sync(0xffffffffu, (int)(threadIdx.x >> 5), 0);
-  const bool open = G.open_bc != 0;
+  // VEC 1 runs periodic grids only: the clamp code is compiled out
+  const bool open = VEC != 1 && G.open_bc != 0;
   const int x0 = tx * NW;
   const int y0 = ty * G.lx;
   const int y_end = min(y0 + G.lx, G.ny);
