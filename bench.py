@@ -310,21 +310,23 @@ def run_gpu(args):
     R = max(2, args.e2e_repeats)
     Oh2 = torch.empty_like(Wh).pin_memory()
     outs_h = [Oh if k % 2 == 0 else Oh2 for k in range(R)]
+    # the call's device workspace, allocated once (repeated calls allocate nothing)
+    ws = torch.empty(tg.host_runs_workspace_bytes(W.shape, R), dtype=torch.uint8, device=dev)
     e2e_ms = []
-    for rep in range(4):
+    for rep in range(6):
         barrier()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
         _, its = tg.time_integration_host([Wh] * R, dx, None, GAMMA, False, num_steps=K,
-                                          tile=tile, out=outs_h)
+                                          tile=tile, out=outs_h, workspace=ws)
         b.record(stream)
         barrier()
         assert its == [K] * R
         if rep > 0:
             e2e_ms.append(a.elapsed_time(b))
     e2e_value, e2e = replicas.job_throughput(cells, K * R, min(e2e_ms), world, dev)
-    del Oh2, outs_h
+    del Oh2, outs_h, ws
     torch.cuda.empty_cache()  # the host-run workspace (six states) is not needed again
 
     if rank != 0:

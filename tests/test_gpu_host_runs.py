@@ -111,3 +111,21 @@ def test_runs_on_the_callers_stream(tg):
     assert float(prior[-1]) == float(1 << 22)
     for o, r in zip(outs, refs):
         assert torch.equal(o, r)
+
+
+def test_caller_workspace_is_reused(tg):
+    """A workspace passed by the caller serves repeated calls (no device
+    allocation per call) with the same results; one too small is rejected."""
+    shape = (20, 18, 32)
+    states = [random_state(shape, 70 + k).pin_memory() for k in range(3)]
+    ws = torch.empty(tg.host_runs_workspace_bytes(shape, 3), dtype=torch.uint8, device="cuda")
+    first, _ = tg.time_integration_host(states, 0.05, None, GAMMA, False, num_steps=4,
+                                        workspace=ws)
+    again, _ = tg.time_integration_host(states, 0.05, None, GAMMA, False, num_steps=4,
+                                        workspace=ws)
+    for a, b, s in zip(first, again, states):
+        assert torch.equal(a, b)
+        assert torch.equal(a, tg.run_steps(s.cuda(), 0.05, GAMMA, 4).cpu())
+    with pytest.raises(ValueError):
+        tg.time_integration_host(states, 0.05, None, GAMMA, False, num_steps=4,
+                                 workspace=ws[:1024])

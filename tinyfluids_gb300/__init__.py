@@ -15,7 +15,8 @@ from .fluid import (DENSITY_INDEX, PRESSURE_INDEX, VAR_AXIS, VELOCITY_X_INDEX,  
                     primitive_state_from_conserved, resolved_tile, set_exact,
                     speed_of_sound)
 from .initial_conditions import overpressure, setup_ics, shear_layer  # noqa: F401
-from .time_integration import run_steps, step, time_integration_host  # noqa: F401
+from .time_integration import (host_runs_workspace_bytes, run_steps, step,  # noqa: F401
+                               time_integration_host)
 from .time_integration import time_integration as time_integration_fn  # noqa: F401
 from ._lib import TinyfluidsError, library_path  # noqa: F401
 

@@ -22,6 +22,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <utility>
 #include <vector>
 
@@ -38,6 +39,34 @@ static unsigned long long slot_state_bytes(int nx, int ny, int nz) {
   const unsigned long long n = (unsigned long long)nx * ny * nz;
   if (n > (1ull << 40)) return 0;
   return align256(5ull * sizeof(float) * n);
+}
+
+// The two copy streams of a device (host-to-device, device-to-host), created
+// on first use and kept for the life of the process, so a call creates no
+// streams.  Calls on one device share them, which only orders their copies.
+static std::mutex g_copy_mu;
+static std::vector<std::pair<cudaStream_t, cudaStream_t>> g_copy_streams;
+
+static int copy_streams(cudaStream_t* up, cudaStream_t* down) {
+  int dev = 0;
+  TF_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
+  std::lock_guard<std::mutex> lk(g_copy_mu);
+  if ((int)g_copy_streams.size() <= dev) g_copy_streams.resize((size_t)dev + 1, {nullptr, nullptr});
+  auto& p = g_copy_streams[(size_t)dev];
+  if (!p.first) {
+    // non-blocking: no implicit ordering against the legacy default stream
+    TF_TRY(cuda_check(cudaStreamCreateWithFlags(&p.first, cudaStreamNonBlocking),
+                      "cudaStreamCreate"));
+    if (cuda_check(cudaStreamCreateWithFlags(&p.second, cudaStreamNonBlocking),
+                   "cudaStreamCreate") != TF_OK) {
+      cudaStreamDestroy(p.first);
+      p.first = nullptr;
+      return TF_ERR_CUDA;
+    }
+  }
+  *up = p.first;
+  *down = p.second;
+  return TF_OK;
 }
 
 }  // namespace tf
@@ -119,9 +148,7 @@ extern "C" int tf_time_integration_host(const float* const* W_in_host, float* co
     return st != TF_OK;
   };
   do {
-    // non-blocking: no implicit ordering against the legacy default stream
-    if (fail(cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking), "cudaStreamCreate")) break;
-    if (fail(cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking), "cudaStreamCreate")) break;
+    if ((st = copy_streams(&up, &down)) != TF_OK) break;
     bool ok = true;
     for (int i = 0; i < 7 && ok; ++i)
       ok = !fail(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming), "cudaEventCreate");
@@ -180,7 +207,5 @@ extern "C" int tf_time_integration_host(const float* const* W_in_host, float* co
   }
   for (int i = 0; i < 7; ++i)
     if (ev[i]) cudaEventDestroy(ev[i]);
-  if (up) cudaStreamDestroy(up);
-  if (down) cudaStreamDestroy(down);
   return st;
 }

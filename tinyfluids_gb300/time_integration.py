@@ -68,7 +68,7 @@ def step(primitive_state, grid_spacing, gamma, C_CFL=0.4, handle_boundaries=Fals
 
 def time_integration_host(primitive_states, grid_spacing, t_final, gamma, handle_boundaries,
                           *, num_steps=None, C_CFL=0.4, dt=None, exact=None, tile=None,
-                          out=None, device=None):
+                          out=None, device=None, workspace=None):
     """time_integration.py:94-128 for host-resident states: each CPU state of
     ``primitive_states`` (a list of [5, nx, ny, nz] float32 CPU tensors or
     numpy arrays of one shape, or one such state) is copied to the GPU, run with exactly
@@ -78,7 +78,9 @@ def time_integration_host(primitive_states, grid_spacing, t_final, gamma, handle
     device's step rate.  Returns ``(states, num_iterations)``: lists of CPU
     tensors (pinned; ``out`` may name them, including the inputs themselves
     for an in-place update) and ints.  Blocks until the outputs are in host
-    memory."""
+    memory.  ``workspace``: a uint8 CUDA tensor of at least
+    ``host_runs_workspace_bytes(shape, count)`` bytes to use instead of one
+    allocated per call (repeated calls then allocate nothing on the device)."""
     single = isinstance(primitive_states, (torch.Tensor, np.ndarray))
     states = [primitive_states] if single else list(primitive_states)
     if not states:
@@ -129,7 +131,15 @@ def time_integration_host(primitive_states, grid_spacing, t_final, gamma, handle
         nbytes = int(lib.tf_host_runs_workspace_bytes(nx, ny, nz, n))
         if nbytes == 0:
             raise ValueError(f"invalid grid {shape[1:]}")
-        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        if workspace is None:
+            ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        else:
+            ws = workspace
+            if (not isinstance(ws, torch.Tensor) or not ws.is_cuda or ws.device != dev
+                    or not ws.is_contiguous() or ws.numel() * ws.element_size() < nbytes):
+                raise ValueError(f"workspace must be a contiguous CUDA tensor on {dev} of at "
+                                 f"least {nbytes} bytes")
+            nbytes = ws.numel() * ws.element_size()
         ins = (_lib.vp * n)(*[st.data_ptr() for st in states])
         ous = (_lib.vp * n)(*[o.data_ptr() for o in outs])
         its = (_lib.c_int * n)()
@@ -139,6 +149,13 @@ def time_integration_host(primitive_states, grid_spacing, t_final, gamma, handle
                   nbytes, its, torch.cuda.current_stream(dev).cuda_stream)
     iters = list(its)
     return (outs[0], iters[0]) if single else (outs, iters)
+
+
+def host_runs_workspace_bytes(shape, count):
+    """Device workspace bytes ``time_integration_host`` needs for ``count``
+    states of ``shape`` ([5,] nx, ny, nz)."""
+    nx, ny, nz = (int(v) for v in tuple(shape)[-3:])
+    return int(_lib.load().tf_host_runs_workspace_bytes(nx, ny, nz, int(count)))
 
 
 def _run(primitive_state, grid_spacing, gamma, t_final, max_steps, fixed_dt,
