@@ -15,7 +15,12 @@
  *    CUDA graph, whose resources the CUDA driver holds).  Inputs are never
  *    modified; outputs must not alias inputs.
  *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Work is
- *    enqueued asynchronously unless stated otherwise.
+ *    enqueued asynchronously unless stated otherwise.  The fused step
+ *    kernels are launched with programmatic stream serialization: each waits
+ *    for the work before it, and lets the next launch start early, so a
+ *    caller's kernel launched after them with that attribute must call
+ *    cudaGridDependencySynchronize() before reading their output (ordinary
+ *    launches, copies and events are ordered as usual).
  *  - Every function returns a tf_status; tf_last_error() describes the last
  *    failure on the calling thread.
  *
