@@ -130,6 +130,9 @@ def test_host_state_runs_check_arguments_before_any_copy(lib):
 def test_host_state_api_validates_before_launch():
     import torch
     import tinyfluids_gb300 as tg
+    sb = (5 * 4 * 32 ** 3 + 255) // 256 * 256
+    assert tg.host_runs_workspace_bytes((5, 32, 32, 32), 3) == 6 * sb + 256
+    assert tg.host_runs_workspace_bytes((32, 32, 32), 3) == 6 * sb + 256
     good = torch.zeros(5, 4, 4, 4)
     with pytest.raises(ValueError):
         tg.time_integration_host([], 0.1, 0.2, 5 / 3, False)
@@ -144,6 +147,8 @@ def test_host_state_api_validates_before_launch():
         tg.time_integration_host([good], 0.1, 0.2, 5 / 3, False, out=[good, good])
     with pytest.raises(ValueError):
         tg.time_integration_host([good], 0.1, 0.2, 5 / 3, False, num_steps=-1)
+    with pytest.raises(ValueError):  # a fixed dt must be positive
+        tg.time_integration_host([good], 0.1, 0.2, 5 / 3, False, dt=-1.0)
 
 
 def test_product_library_is_not_the_checked_build(lib):
